@@ -1,0 +1,463 @@
+#!/usr/bin/env python3
+"""Benchmark: 32^4 SU(3) stout-smeared HMC trajectories per second on one GB300.
+
+Workload (one "step" = one HMC trajectory): 32^4 lattice, Haar-random start
+(seed 7), Wilson action beta = 6.0 evaluated on 2-level stout-smeared links
+(rho = 0.1), tau = 1 with 20 QPQ steps, momentum refresh + Metropolis test.
+The headline form is mixed precision: staples, force and stout forward/adjoint
+in fp32 on 12-real links; Hamiltonian, Delta H, link updates and
+re-unitarisation in fp64. The plain fp64 form is timed beside it.
+
+  python bench.py [--gpus N --steps K --warmup W]      # this library
+  python bench.py --impl reference [...]               # CPU oracle port
+Prints one JSON line (rank 0).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "32^4 stout-HMC traj/s: FP32-force+adjoint vs FP64, 1 GB300, |ΔH err|≤1e-4"
+UNIT = "traj/s"
+BETA = 6.0
+RHO = (0.1, 0.1)
+TAU = 1.0
+NSTEPS = 20
+SEED = 7
+L2_BYTES = 129 * 1024 * 1024
+
+
+def workload_name(L):
+    return "%d^4 SU(3) HMC, Wilson beta=6.0 on 2-level stout (rho=0.1) links, tau=1, 20 QPQ steps, Haar start seed 7" % L
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes / flops per link of every kernel class (compulsory traffic:
+# each input field read once, each output written once). fp32 12-real link =
+# 48 B, fp32 3x3 matrix = 72 B, fp64 link = 144 B, fp64 momenta = 64 B.
+# ---------------------------------------------------------------------------
+def algorithmic_bytes_per_link(kclass, precision):
+    if precision == "mixed":
+        link, mat = 48, 72
+    else:
+        link, mat = 144, 144
+    return {
+        # U in, Ubar out, C out
+        "stout_fwd": link + link + mat,
+        # U, C, Dbar in (top level: Ubar_top in); Z, Dp out -- mean of the two levels
+        "bwd_local": (link + mat + mat + 2 * mat + link + mat + link + 2 * mat) / 2.0,
+        # U, Z, Dp in; D out (upper level) or P read+write (bottom level) -- mean
+        "bwd_gather": (link + 2 * mat + mat + link + 2 * mat + 128) / 2.0,
+        # P in, U in/out (fp64), fp32 shadow out
+        "link_update": 64 + 144 + 144 + (48 if precision == "mixed" else 0),
+        "plaquette": 144,
+        "force": link + 128,
+    }.get(kclass)
+
+
+def algorithmic_flops_per_link(kclass):
+    """3x3 complex products counted at 198 flops (216 with accumulation)."""
+    mm, mac, rec = 198, 216, 42
+    staples = 6 * (mm + mac)  # six staples, two products each
+    return {
+        "stout_fwd": staples + 2 * mm + 600,            # + U S, exp (series + Qh^2), E U
+        "bwd_local": (staples / 2.0) + 8 * mm + 900,      # mean: top level rebuilds staples
+        "bwd_gather": 3 * 6 * (mm + mac) + 18 * rec + mm / 2.0,
+        "link_update": 2 * mm + 400,
+        "plaquette": 2 * mm * 6 / 4.0,
+        "force": staples + mm,
+    }.get(kclass)
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# measured compute peaks (cuBLAS sgemm without TF32, dgemm), burst
+# ---------------------------------------------------------------------------
+def measure_gemm_peaks(torch):
+    out = {}
+    torch.backends.cuda.matmul.allow_tf32 = False
+    for name, dt, n in (("fp32_tflops", torch.float32, 8192), ("fp64_tflops", torch.float64, 4096)):
+        a = torch.randn(n, n, dtype=dt, device="cuda")
+        b = torch.randn(n, n, dtype=dt, device="cuda")
+        for _ in range(2):
+            torch.matmul(a, b)
+        torch.cuda.synchronize()
+        best = 1e30
+        for _ in range(3):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            torch.matmul(a, b)
+            e.record()
+            e.synchronize()
+            best = min(best, s.elapsed_time(e) / 1e3)
+        out[name] = 2 * n ** 3 / best / 1e12
+        del a, b
+    torch.cuda.empty_cache()
+    return out
+
+
+def read_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "of measured (MEASURED_PEAKS.json hbm_gbs)"
+    return 6800.0, "of fallback (6.8 TB/s)"
+
+
+def read_traffic(kclass, precision, L):
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    key = "%s/%s/%d" % (kclass, precision, L)
+    return d.get(key)
+
+
+# ---------------------------------------------------------------------------
+# this library
+# ---------------------------------------------------------------------------
+def make_setup(pkg, L, precision, seed):
+    U = pkg.gauge_configuration((L,) * 4, start="hot", seed=seed)
+    P = pkg.gauge_momenta(U)
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, BETA / 2, "plaquette")
+    net = pkg.CovNeuralnet(U)
+    for r in RHO:
+        pkg.push_(net, pkg.STOUT_Layer("plaquette", r))
+    drv = pkg.md_driver(U, action, steps=NSTEPS, trajectory_length=TAU, smearing=net, precision=precision)
+    return U, P, drv
+
+
+def timed_hmc(pkg, torch, U, P, drv, steps, warmup, rank, dist, prof=False):
+    import numpy as np
+    from gaugefields_gb300 import _lib
+    import ctypes
+    lib = _lib.load()
+    stream = torch.cuda.Stream()
+    U.ctx.set_stream(stream.cuda_stream)
+    U.ctx.torch_stream = stream  # keep the stream alive as long as the context
+    rng = np.random.RandomState(1000 + rank)
+    sweep = 0
+    for _ in range(warmup):
+        pkg.hmc_update_(U, P, drv, seed=SEED + 101 * rank, sweep=sweep, unif=rng.uniform())
+        sweep += 1
+    if prof:
+        lib.gf_prof_enable(U.ctx.h, 1)
+    n0 = ctypes.c_longlong()
+    lib.gf_launch_count(ctypes.byref(n0))
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    dhs, acc = [], 0
+    for _ in range(steps):
+        r = pkg.hmc_update_(U, P, drv, seed=SEED + 101 * rank, sweep=sweep, unif=rng.uniform())
+        dhs.append(r.delta_hamiltonian)
+        acc += int(r.accepted)
+        sweep += 1
+    e.record(stream)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    sec = s.elapsed_time(e) / 1e3
+    n1 = ctypes.c_longlong()
+    lib.gf_launch_count(ctypes.byref(n1))
+    kern = {}
+    if prof:
+        for k, name in enumerate(_lib.KERNEL_CLASSES):
+            ms, cnt = ctypes.c_double(), ctypes.c_longlong()
+            lib.gf_prof_read(U.ctx.h, k, ctypes.byref(ms), ctypes.byref(cnt))
+            if cnt.value:
+                kern[name] = {"ms": ms.value, "launches": cnt.value}
+        lib.gf_prof_enable(U.ctx.h, 0)
+    return sec, n1.value - n0.value, kern, dhs, acc
+
+
+def e2e_hmc(pkg, torch, L, steps, warmup, rank):
+    """Same metric through the C-ABI with host buffers: every step uploads the
+    links and the step's momenta from pinned host memory (reference layout),
+    runs md_trajectory!, applies Metropolis on the host and downloads the links."""
+    import ctypes
+    import numpy as np
+    from gaugefields_gb300 import _lib
+    V = L ** 4
+    U, P, drv = make_setup(pkg, L, "mixed", SEED + 101 * rank)
+    lib = _lib.load()
+    hU = torch.empty((4, V, 3, 3), dtype=torch.complex128, pin_memory=True).numpy()
+    hP = torch.empty((4, V, 8), dtype=torch.float64, pin_memory=True).numpy()
+    hR = torch.empty((4, V, 3, 3), dtype=torch.complex128, pin_memory=True).numpy()
+    hU[...] = U.to_host()
+    rng = np.random.RandomState(77 + rank)
+    moms = []
+    for k in range(2):
+        pkg.gaussian_momenta_(P, seed=SEED, sweep=1000 + k)
+        moms.append(P.to_host())
+    prm = drv.params()
+    out = (ctypes.c_double * 3)()
+
+    def step(k):
+        hP[...] = moms[k % 2]
+        _lib.check(lib.gf_upload_links(U.ctx.h, U.field.h, ctypes.c_void_p(hU.ctypes.data)), U.ctx.h)
+        _lib.check(lib.gf_upload_mom(U.ctx.h, P.field.h, ctypes.c_void_p(hP.ctypes.data)), U.ctx.h)
+        _lib.check(lib.gf_md_trajectory(U.ctx.h, U.field.h, P.field.h, ctypes.byref(prm), out), U.ctx.h)
+        if rng.uniform() < np.exp(-out[2]):
+            _lib.check(lib.gf_download_links(U.ctx.h, U.field.h, ctypes.c_void_p(hU.ctypes.data)), U.ctx.h)
+        else:
+            # rejected: the host links stay; the result read back is the same size
+            _lib.check(lib.gf_download_links(U.ctx.h, U.field.h, ctypes.c_void_p(hR.ctypes.data)), U.ctx.h)
+        return out[2]
+
+    for k in range(warmup):
+        step(k)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(steps):
+        step(k)
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    return {"value": steps / sec, "unit": UNIT, "h2d_bytes_per_step": 36 * V * 16 + 32 * V * 8,
+            "d2h_bytes_per_step": 36 * V * 16 + 3 * 8, "ms_per_step": 1e3 * sec / steps}
+
+
+def dh_check(pkg, L):
+    """Delta H of one trajectory from the same start and momenta in both forms."""
+    res = {}
+    for prec in ("fp64", "mixed"):
+        U, P, drv = make_setup(pkg, L, prec, SEED)
+        pkg.gaussian_momenta_(P, seed=SEED, sweep=0)
+        res[prec] = pkg.md_trajectory_(U, P, drv).delta_hamiltonian
+    return {"dH_fp64": res["fp64"], "dH_mixed": res["mixed"], "abs_diff": abs(res["mixed"] - res["fp64"]),
+            "start": "Haar seed 7 (unthermalised), momenta seed 7"}
+
+
+def oracle_sample(threads, L_sample=16, md_steps=None):
+    """Returns (seconds per 32^4 trajectory, description)."""
+    import __graft_entry__ as entry
+    O = entry.load_oracle()
+    O.build()
+    O.set_threads(threads)
+    Ls = [L_sample] * 4
+    U = O.hot_start(Ls, SEED)
+    P = O.gauss_mom(Ls, SEED, 0)
+    scale = (32 / L_sample) ** 4
+    if md_steps is None:
+        t0 = time.perf_counter()
+        O.md_trajectory(Ls, U, P, BETA, TAU, NSTEPS, "QPQ", rho=list(RHO))
+        t = time.perf_counter() - t0
+        desc = "one full trajectory (20 QPQ steps + 2 H) at %d^4, time x %g (cost scales with sites)" % (L_sample, scale)
+        return t * scale, desc
+    t0 = time.perf_counter()
+    O.md_steps(Ls, U, P, BETA, TAU / NSTEPS, md_steps, rho=list(RHO))
+    t_step = (time.perf_counter() - t0) / md_steps
+    return t_step, None
+
+
+def max_over_ranks(torch, dist, seconds, device):
+    """Replicas only: every rank runs its own chain; the job time is the
+    slowest rank's and the job value counts the trajectories of all ranks."""
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args):
+    """--impl reference: the oracle port of the reference's CPU path, timed on
+    all host cores; each step is a bounded sample (one MD step at 16^4)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import __graft_entry__ as entry
+    O = entry.load_oracle()
+    O.build()
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    Ls = [16] * 4
+    U = O.hot_start(Ls, SEED)
+    P = O.gauss_mom(Ls, SEED, 0)
+    t0 = time.perf_counter()
+    O.hamiltonian(Ls, U, P, BETA, list(RHO))
+    t_h = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        O.md_steps(Ls, U, P, BETA, TAU / NSTEPS, 1, rho=list(RHO))
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.md_steps(Ls, U, P, BETA, TAU / NSTEPS, 1, rho=list(RHO))
+    t_step = (time.perf_counter() - t0) / args.steps
+    scale = (32 / 16) ** 4
+    t_traj = scale * (NSTEPS * t_step + 2 * t_h)
+    value = 1.0 / t_traj
+    sample = ("each step: one QPQ MD step (2 link updates + stout force) of the 16^4 lattice; trajectory time = "
+              "16 x (20 x step + 2 x Hamiltonian) (cost scales with sites)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_traj, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (Haar start, seed 7)",
+            "config": {"workload": workload_name(32), "lattice": [32] * 4, "precision": "fp64 (CPU oracle)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--lattice", type=int, default=32)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    import __graft_entry__ as entry
+    pkg = entry.build()
+    L = args.lattice
+    V = L ** 4
+
+    peaks = measure_gemm_peaks(torch)
+    hbm_peak, hbm_note = read_peaks()
+
+    # headline: mixed precision
+    U, P, drv = make_setup(pkg, L, "mixed", SEED + 101 * rank)
+    clk = ClockSampler(local)
+    clk.start()
+    sec, launches, kern, dhs, acc = timed_hmc(pkg, torch, U, P, drv, args.steps, args.warmup, rank, dist, prof=True)
+    clocks = clk.stop()
+    del U, P, drv
+    tmax = max_over_ranks(torch, dist, sec, "cuda")
+    value = world * args.steps / tmax
+
+    # plain fp64 form of the same workload
+    fp64 = None
+    if not args.no_fp64:
+        U, P, drv = make_setup(pkg, L, "fp64", SEED + 101 * rank)
+        s64, _, _, _, _ = timed_hmc(pkg, torch, U, P, drv, 1, 1, rank, None)
+        fp64 = {"value": 1.0 / s64, "unit": UNIT, "ms_per_step": 1e3 * s64, "steps": 1, "warmup": 1}
+        del U, P, drv
+    dh = dh_check(pkg, L) if not args.no_fp64 else None
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = e2e_hmc(pkg, torch, L, max(2, min(args.steps, 3)), 1, rank)
+
+    # roofline of the dominant kernel (device time from CUDA events in the timed region)
+    roof, compute = None, None
+    if kern:
+        dom = max(kern, key=lambda k: kern[k]["ms"])
+        d = kern[dom]
+        per_launch_s = d["ms"] / d["launches"] / 1e3
+        bpl = algorithmic_bytes_per_link(dom, "mixed")
+        alg_bytes = bpl * 4 * V
+        achieved = alg_bytes / per_launch_s / 1e9
+        roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "peak_note": hbm_note, "algorithmic_bytes_per_launch": alg_bytes,
+                "traffic": read_traffic(dom, "mixed", L), "launches": d["launches"],
+                "avg_launch_ms": 1e3 * per_launch_s}
+        fl = algorithmic_flops_per_link(dom) * 4 * V
+        compute = {"kernel": dom, "achieved_tflops": fl / per_launch_s / 1e12, "peak_tflops": peaks["fp32_tflops"],
+                   "peak_note": "cuBLAS sgemm (no TF32) measured in this run", "flops_per_launch": fl,
+                   "frac": fl / per_launch_s / 1e12 / peaks["fp32_tflops"]}
+        total_ms = sum(v["ms"] for v in kern.values())
+        for k in kern:
+            kern[k]["share"] = kern[k]["ms"] / total_ms
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        cores = os.cpu_count() or 1
+        t_traj, desc = oracle_sample(cores)
+        cpu = {"value": 1.0 / t_traj, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * tmax / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (Haar-random SU(3) start, seed 7; Gaussian momenta per trajectory)",
+            "config": {"workload": workload_name(L), "lattice": [L] * 4, "precision": "mixed",
+                       "replicas": world, "l2": "inputs larger than L2: fp64 links %d MB + fp32 links %d MB"
+                       % (36 * V * 16 >> 20, 12 * V * 4 >> 20)},
+            "e2e": e2e, "gpu_launches": launches, "roofline": roof, "compute": compute, "cpu_baseline": cpu,
+            "clocks": clocks, "fp64_form": fp64,
+            "mixed_over_fp64": (value / world) / fp64["value"] if fp64 else None,
+            "dH_check": dh, "kernels": kern, "gemm_peaks": peaks,
+            "accepted": acc, "dH_timed": dhs,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

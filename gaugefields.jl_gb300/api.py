@@ -1,0 +1,614 @@
+"""Host-side mirror of the Gaugefields.jl interface for the SU(3) hot path.
+
+Names follow the reference (Julia `f!` becomes Python `f_`); every call goes
+through the C-ABI of libgfgb300.so, so the CUDA kernels do all the arithmetic.
+Reference citations are paths inside Gaugefields.jl.
+
+Host arrays use the reference's layouts (see include/gaugefields_gb300.h):
+  links   : complex128 array (4, V, 3, 3) indexed [mu, lex, j, i]
+            (the column-major (3,3,NX,NY,NZ,NT) array of each direction)
+  momenta : float64 array (4, V, 8) indexed [mu, lex, a]
+"""
+import ctypes
+import math
+import os
+from collections import namedtuple
+
+import numpy as np
+
+from . import _lib
+from ._lib import MDParams, call
+
+__all__ = [
+    "GB300Backend", "gauge_configuration", "measure_plaquette", "calculate_Plaquette", "construct_staple_",
+    "gauge_momenta", "gaussian_momenta_", "gaussian_momenta", "GaugeAction", "push_", "evaluate_GaugeAction",
+    "QPQ", "PQP", "md_driver", "md_step_size", "md_hamiltonian", "md_potential", "md_force_",
+    "md_action_workspace", "update_gaugefields_", "update_momenta_", "md_step_", "md_trajectory_",
+    "hmc_update_", "STOUT_Layer", "CovNeuralnet", "stout_smearing", "smear", "calc_smearedU", "back_prop",
+    "Gradientflow", "gradient_flow", "flow_", "add_force_", "energy_density_plaquette", "substitute_U_",
+    "similar", "clear_U_",
+]
+
+
+class GB300Backend:
+    """Backend selector for gauge_configuration (cf. LatticeMatricesBackend,
+    src/API.jl:6-27): one GB300, even/odd SoA storage, no halo, no MPI."""
+
+    def __init__(self, device=0):
+        self.device = int(device)
+
+
+class _Context:
+    """Owns one gf_ctx (lattice geometry + stream + reduction scratch)."""
+
+    def __init__(self, L, device=0):
+        lib = _lib.load()
+        arr = (ctypes.c_int * 4)(*[int(x) for x in L])
+        h = ctypes.c_void_p()
+        rc = lib.gf_ctx_create(arr, int(device), ctypes.byref(h))
+        _lib.check(rc, None)
+        self.h = h
+        self.L = tuple(int(x) for x in L)
+        self.V = int(np.prod(self.L))
+        self.device = device
+
+    def sync(self):
+        call("gf_ctx_synchronize", self.h, ctx=self.h)
+
+    def set_stream(self, stream_handle):
+        call("gf_ctx_set_stream", self.h, ctypes.c_void_p(stream_handle), ctx=self.h)
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None) and _lib._lib is not None:
+                _lib._lib.gf_ctx_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+class _Field:
+    def __init__(self, ctx, kind):
+        self.ctx = ctx
+        self.kind = kind
+        h = ctypes.c_void_p()
+        call("gf_field_alloc", ctx.h, int(kind), ctypes.byref(h), ctx=ctx.h)
+        self.h = h
+
+    def device_ptr(self):
+        p = ctypes.c_void_p()
+        call("gf_field_device_ptr", self.h, ctypes.byref(p))
+        return p.value
+
+    def nbytes(self):
+        n = ctypes.c_size_t()
+        call("gf_field_bytes", self.h, ctypes.byref(n))
+        return n.value
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None) and _lib._lib is not None:
+                _lib._lib.gf_field_free(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class Gaugefields4D:
+    """U: the four SU(3) link directions of a 4D lattice on the GPU
+    (Gaugefields_4D_MPILattice, src/4D/mpi_jacc/gaugefields_4D_MPILattice.jl:34-121).
+    kind GF_LINK64 (complex128) or GF_MAT64 for general matrices."""
+
+    NC = 3
+    Dim = 4
+
+    def __init__(self, ctx, kind=_lib.GF_LINK64):
+        self.ctx = ctx
+        self.field = _Field(ctx, kind)
+
+    @property
+    def L(self):
+        return self.ctx.L
+
+    @property
+    def NV(self):
+        return self.ctx.V
+
+    def __len__(self):
+        return 4
+
+    def similar(self):
+        return Gaugefields4D(self.ctx, self.field.kind)
+
+    def to_host(self):
+        out = np.empty((4, self.NV, 3, 3), dtype=np.complex128)
+        call("gf_download_links", self.ctx.h, self.field.h, _ptr(out), ctx=self.ctx.h)
+        return out
+
+    def from_host(self, arr):
+        arr = np.ascontiguousarray(arr, dtype=np.complex128)
+        if arr.size != 36 * self.NV:
+            raise ValueError("link array has %d elements; expected %d" % (arr.size, 36 * self.NV))
+        call("gf_upload_links", self.ctx.h, self.field.h, _ptr(arr), ctx=self.ctx.h)
+        return self
+
+
+class TAGaugefields4D:
+    """Conjugate momenta / forces: 8 su(3) coefficients per link
+    (TA_Gaugefields_4D_MPILattice, src/4D/mpi_jacc/TA_gaugefields_4D_MPILattice.jl:4-72)."""
+
+    NumofBasis = 8
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        self.field = _Field(ctx, _lib.GF_MOM64)
+
+    def __len__(self):
+        return 4
+
+    def similar(self):
+        return TAGaugefields4D(self.ctx)
+
+    def to_host(self):
+        out = np.empty((4, self.ctx.V, 8), dtype=np.float64)
+        call("gf_download_mom", self.ctx.h, self.field.h, _ptr(out), ctx=self.ctx.h)
+        return out
+
+    def from_host(self, arr):
+        arr = np.ascontiguousarray(arr, dtype=np.float64)
+        if arr.size != 32 * self.ctx.V:
+            raise ValueError("momentum array has %d elements; expected %d" % (arr.size, 32 * self.ctx.V))
+        call("gf_upload_mom", self.ctx.h, self.field.h, _ptr(arr), ctx=self.ctx.h)
+        return self
+
+    def __mul__(self, other):
+        """P*P = sum_a p_a^2 (TA_gaugefields_4D_serial.jl:106-129). Only the
+        self product (the kinetic term) is provided on the device."""
+        if other is not self:
+            raise NotImplementedError("only P*P (the kinetic term) is provided")
+        out = ctypes.c_double()
+        call("gf_kinetic", self.ctx.h, self.field.h, ctypes.byref(out), ctx=self.ctx.h)
+        return out.value
+
+
+# ---------------------------------------------------------------------------
+# configurations and measurements (src/API.jl)
+# ---------------------------------------------------------------------------
+def gauge_configuration(lattice, backend=None, colors=3, halo=1, start="cold", seed=None, eltype=np.complex128,
+                        verbose=0):
+    """gauge_configuration(L; start=:cold|:hot, seed) (src/API.jl:178-251).
+
+    The hot start is Haar-random SU(3) per link (Philox4x32-10 keyed by seed)."""
+    backend = backend or GB300Backend()
+    if not isinstance(backend, GB300Backend):
+        raise ValueError("this package provides the GB300Backend only")
+    L = tuple(int(x) for x in lattice)
+    if len(L) != 4:
+        raise ValueError("the GB300 backend is 4D; got %d dimensions" % len(L))
+    if any(x <= 0 for x in L):
+        raise ValueError("lattice extents must be positive; got %s" % (L,))
+    if colors != 3:
+        raise ValueError("the GB300 backend implements SU(3) only; got colors=%d" % colors)
+    if halo < 0:
+        raise ValueError("halo must be nonnegative; got %d" % halo)
+    if start not in ("cold", "hot"):
+        raise ValueError("start must be :cold or :hot; got %s" % start)
+    if np.dtype(eltype) != np.complex128:
+        raise ValueError("gauge_configuration stores complex128 links; use md_driver(precision='mixed') for fp32")
+    ctx = _Context(L, backend.device)
+    U = Gaugefields4D(ctx)
+    if start == "cold":
+        call("gf_cold_start", ctx.h, U.field.h, ctx=ctx.h)
+    else:
+        if seed is None:
+            seed = int.from_bytes(os.urandom(8), "little")
+        call("gf_hot_start", ctx.h, U.field.h, ctypes.c_uint64(int(seed)), ctx=ctx.h)
+    return U
+
+
+def similar(U):
+    return U.similar()
+
+
+def substitute_U_(A, B):
+    """substitute_U!(A, B): A <- B (src/4D/mpi_jacc/gaugefields_4D_MPILattice.jl:509)."""
+    call("gf_field_copy", A.ctx.h, A.field.h, B.field.h, ctx=A.ctx.h)
+
+
+def clear_U_(A):
+    call("gf_field_zero", A.ctx.h, A.field.h, ctx=A.ctx.h)
+
+
+def calculate_Plaquette(U, temp=None, staple=None):
+    """Sum over mu of Re tr(U_mu V_mu^dag)/2 (src/AbstractGaugefields.jl:2684-2699)."""
+    out = ctypes.c_double()
+    call("gf_plaquette", U.ctx.h, U.field.h, ctypes.byref(out), ctx=U.ctx.h)
+    return out.value
+
+
+def measure_plaquette(U, normalize=True):
+    """measure_plaquette (src/API.jl:395-404): divided by 6*V*NC by default."""
+    value = calculate_Plaquette(U)
+    if not normalize:
+        return value
+    return value / (6 * U.NV * 3)
+
+
+def energy_density_plaquette(U):
+    """Plaquette-defined E = 2 sum_{mu<nu} Re tr(1 - P_munu) per site = 36 (1 - <P>)."""
+    return 36.0 * (1.0 - measure_plaquette(U))
+
+
+def construct_staple_(V, U, mu, temp=None):
+    """construct_staple!(V, U, mu) (src/AbstractGaugefields.jl:2873-2923), mu 1-based
+    as in the reference; the staple is written into direction slot mu of V."""
+    if not 1 <= mu <= 4:
+        raise ValueError("mu must be in 1..4")
+    call("gf_staple", U.ctx.h, U.field.h, int(mu) - 1, V.field.h, ctx=U.ctx.h)
+    return V
+
+
+def gauge_momenta(U):
+    """Zero-valued momenta compatible with U (src/API.jl:333)."""
+    P = TAGaugefields4D(U.ctx)
+    call("gf_field_zero", U.ctx.h, P.field.h, ctx=U.ctx.h)
+    return P
+
+
+def gaussian_momenta_(momenta, sigma=1.0, seed=None, sweep=0):
+    """gaussian_momenta!(P; seed, sweep) (src/API.jl:341-368): p_a ~ N(0, sigma^2)."""
+    if sweep < 0:
+        raise ValueError("sweep must be nonnegative; got %d" % sweep)
+    if sigma != 1.0:
+        raise ValueError("the device generator draws unit-variance momenta")
+    if seed is None:
+        seed = int.from_bytes(os.urandom(8), "little")
+    P = momenta
+    call("gf_gaussian_momenta", P.ctx.h, P.field.h, ctypes.c_uint64(int(seed)), ctypes.c_uint64(int(sweep)),
+         ctx=P.ctx.h)
+    return P
+
+
+def gaussian_momenta(U, sigma=1.0, seed=None, sweep=0):
+    return gaussian_momenta_(gauge_momenta(U), sigma=sigma, seed=seed, sweep=sweep)
+
+
+# ---------------------------------------------------------------------------
+# gauge action (src/action/GaugeActions.jl)
+# ---------------------------------------------------------------------------
+class GaugeAction:
+    """Wilson-loop action. The GB300 backend implements the Wilson plaquette
+    action push!(action, beta/2, plaq U plaq^dag) (docs/src/hmc.md:146-150)."""
+
+    def __init__(self, U, hascovnet=False):
+        self.terms = []
+        self.hascovnet = hascovnet
+
+    @property
+    def beta(self):
+        return 2.0 * sum(c for c, _ in self.terms)
+
+
+def push_(action_or_net, coefficient, loops=None):
+    """push!(action, coefficient, loops) / push!(network, layer)."""
+    if isinstance(action_or_net, CovNeuralnet):
+        action_or_net.layers.append(coefficient)
+        return action_or_net
+    if loops not in ("plaquette", ("plaquette", "plaquette_dag")):
+        raise ValueError("the GB300 backend supports the plaquette loops (with their conjugates) only")
+    c = float(coefficient.real) if isinstance(coefficient, complex) else float(coefficient)
+    action_or_net.terms.append((c, loops))
+    return action_or_net
+
+
+def evaluate_GaugeAction(action, U):
+    """Traced lattice sum of the action's loops (GaugeActions.jl:132-142):
+    beta/2 * sum tr(plaq + plaq^dag) = beta * sum Re tr P."""
+    return action.beta * calculate_Plaquette(U)
+
+
+# ---------------------------------------------------------------------------
+# MD driver (src/molecular_dynamics.jl)
+# ---------------------------------------------------------------------------
+class QPQ:
+    """Leapfrog with half link steps at both ends (molecular_dynamics.jl:611-616)."""
+
+
+class PQP:
+    """Leapfrog with half momentum steps at both ends (molecular_dynamics.jl:604-609)."""
+
+
+class MDDriver:
+    def __init__(self, action, integrator, trajectory_length, steps, smearing, precision, reunitarize):
+        self.action = action
+        self.integrator = integrator
+        self.trajectory_length = trajectory_length
+        self.steps = steps
+        self.smearing = smearing
+        self.precision = precision
+        self.reunitarize = reunitarize
+        self._stout = None
+
+    def params(self):
+        p = MDParams()
+        p.beta = self.action.beta
+        p.tau = self.trajectory_length
+        p.steps = self.steps
+        p.integrator = _lib.GF_PQP if isinstance(self.integrator, PQP) else _lib.GF_QPQ
+        p.precision = _lib.GF_MIXED if self.precision == "mixed" else _lib.GF_FP64
+        rho = self.smearing.rhos() if self.smearing is not None else []
+        p.nstout = len(rho)
+        for i, r in enumerate(rho):
+            p.rho[i] = r
+        p.reunitarize = 1 if self.reunitarize else 0
+        return p
+
+
+def md_driver(U, action, steps, trajectory_length=1.0, integrator=None, smearing=None, precision="fp64",
+              reunitarize=True):
+    """md_driver(U, action; steps, trajectory_length, integrator) (molecular_dynamics.jl:440-483).
+
+    smearing: a CovNeuralnet of stout layers; the action is then evaluated on
+    the smeared links and the force is back-propagated to the thin links.
+    precision: "fp64" (plain form) or "mixed" (fp32 force and stout on 12-real
+    links; fp64 Hamiltonian, Delta H, link updates and re-unitarisation)."""
+    integrator = integrator if integrator is not None else QPQ()
+    if len(U) != 4:
+        raise ValueError("the gauge configuration has length %d; expected 4" % len(U))
+    if steps <= 0:
+        raise ValueError("steps must be positive; got %d" % steps)
+    if not math.isfinite(trajectory_length):
+        raise ValueError("trajectory_length must be finite; got %s" % trajectory_length)
+    if trajectory_length == 0:
+        raise ValueError("trajectory_length must not be zero")
+    if precision not in ("fp64", "mixed"):
+        raise ValueError("precision must be 'fp64' or 'mixed'")
+    if not (isinstance(integrator, (QPQ, PQP)) or callable(integrator)):
+        raise ValueError("md_step! is not implemented for %s" % type(integrator).__name__)
+    if not isinstance(action, GaugeAction) or not action.terms:
+        raise ValueError("md_action_workspace is not implemented for %s" % type(action).__name__)
+    return MDDriver(action, integrator, float(trajectory_length), int(steps), smearing, precision, reunitarize)
+
+
+def md_step_size(driver):
+    return driver.trajectory_length / driver.steps
+
+
+def md_action_workspace(action, U):
+    return None
+
+
+def md_potential(action, U, workspace=None, smearing=None):
+    """-Re(evaluate_GaugeAction)/NC (molecular_dynamics.jl:247)."""
+    if smearing is not None:
+        U = smear(U, smearing)
+    out = ctypes.c_double()
+    call("gf_action", U.ctx.h, U.field.h, ctypes.c_double(action.beta), ctypes.byref(out), ctx=U.ctx.h)
+    return out.value
+
+
+def md_force_(force, action, U, workspace=None):
+    """md_force!(F, ::GaugeAction, U, ws) (molecular_dynamics.jl:251-267)."""
+    call("gf_force", U.ctx.h, U.field.h, ctypes.c_double(action.beta), force.field.h, ctx=U.ctx.h)
+    return None
+
+
+def md_hamiltonian(U, P, driver):
+    """Potential (on smeared links if the driver smears) + P*P/2, fp64."""
+    p = driver.params()
+    out = ctypes.c_double()
+    call("gf_hamiltonian", U.ctx.h, U.field.h, P.field.h, ctypes.byref(p), ctypes.byref(out), ctx=U.ctx.h)
+    return out.value
+
+
+def update_gaugefields_(U, P, step_size, driver):
+    """U_mu <- exp(step_size P_mu) U_mu (molecular_dynamics.jl:513-531)."""
+    if not math.isfinite(step_size):
+        raise ValueError("the gauge-field step size must be finite; got %s" % step_size)
+    call("gf_link_update", U.ctx.h, U.field.h, P.field.h, ctypes.c_double(step_size),
+         1 if driver.reunitarize else 0, ctx=U.ctx.h)
+    return U
+
+
+def _stout_for(driver, U):
+    if driver._stout is None:
+        driver._stout = _StoutStack(U.ctx, driver.smearing.rhos(), driver.precision)
+    return driver._stout
+
+
+def update_momenta_(P, U, step_size, driver):
+    """P <- P + step_size * F(U) (molecular_dynamics.jl:539-551)."""
+    if not math.isfinite(step_size):
+        raise ValueError("the momentum step size must be finite; got %s" % step_size)
+    beta = driver.action.beta
+    if driver.smearing is None and driver.precision == "fp64":
+        call("gf_mom_update", U.ctx.h, P.field.h, U.field.h, ctypes.c_double(step_size), ctypes.c_double(beta),
+             ctx=U.ctx.h)
+    elif driver.smearing is None:
+        # mixed precision without smearing: fp32 12-real copy of the links
+        st = driver.__dict__.setdefault("_u32", Gaugefields4D(U.ctx, _lib.GF_LINK32))
+        call("gf_field_copy", U.ctx.h, st.field.h, U.field.h, ctx=U.ctx.h)
+        call("gf_mom_update", U.ctx.h, P.field.h, st.field.h, ctypes.c_double(step_size), ctypes.c_double(beta),
+             ctx=U.ctx.h)
+    else:
+        stack = _stout_for(driver, U)
+        call("gf_stout_mom_update", U.ctx.h, stack.h, P.field.h, U.field.h, ctypes.c_double(step_size),
+             ctypes.c_double(beta), ctx=U.ctx.h)
+    return P
+
+
+def md_step_(integrator, U, P, step_size, driver):
+    """One MD step (molecular_dynamics.jl:593-616). Custom integrators are
+    callables f(U, P, step_size, driver) built from update_momenta_ and
+    update_gaugefields_, as in the reference."""
+    if isinstance(integrator, PQP):
+        update_momenta_(P, U, step_size / 2, driver)
+        update_gaugefields_(U, P, step_size, driver)
+        update_momenta_(P, U, step_size / 2, driver)
+    elif isinstance(integrator, QPQ):
+        update_gaugefields_(U, P, step_size / 2, driver)
+        update_momenta_(P, U, step_size, driver)
+        update_gaugefields_(U, P, step_size / 2, driver)
+    elif callable(integrator):
+        integrator(U, P, step_size, driver)
+    else:
+        raise ValueError("md_step! is not implemented for %s" % type(integrator).__name__)
+
+
+MDResult = namedtuple("MDResult", ["initial_hamiltonian", "final_hamiltonian", "delta_hamiltonian"])
+
+
+def md_trajectory_(U, P, driver, diagnostics=True):
+    """md_trajectory!(U, P, driver) (molecular_dynamics.jl:712-730). The builtin
+    QPQ/PQP run as one native call; custom integrators step from Python."""
+    if isinstance(driver.integrator, (QPQ, PQP)):
+        p = driver.params()
+        out = (ctypes.c_double * 3)()
+        call("gf_md_trajectory", U.ctx.h, U.field.h, P.field.h, ctypes.byref(p), out, ctx=U.ctx.h)
+        return MDResult(out[0], out[1], out[2]) if diagnostics else None
+    h0 = md_hamiltonian(U, P, driver) if diagnostics else None
+    eps = md_step_size(driver)
+    for _ in range(driver.steps):
+        md_step_(driver.integrator, U, P, eps, driver)
+    if not diagnostics:
+        return None
+    h1 = md_hamiltonian(U, P, driver)
+    return MDResult(h0, h1, h1 - h0)
+
+
+HMCResult = namedtuple("HMCResult", ["initial_hamiltonian", "final_hamiltonian", "delta_hamiltonian", "accepted"])
+
+
+def hmc_update_(U, P, driver, seed, sweep, unif):
+    """Momentum refresh + md_trajectory! + Metropolis (docs/src/hmc.md:22-81);
+    a rejected trajectory restores U."""
+    if not isinstance(driver.integrator, (QPQ, PQP)):
+        raise ValueError("hmc_update_ runs the builtin integrators natively")
+    p = driver.params()
+    out = (ctypes.c_double * 4)()
+    call("gf_hmc_update", U.ctx.h, U.field.h, P.field.h, ctypes.byref(p), ctypes.c_uint64(int(seed)),
+         ctypes.c_uint64(int(sweep)), ctypes.c_double(unif), out, ctx=U.ctx.h)
+    return HMCResult(out[0], out[1], out[2], bool(out[3]))
+
+
+# ---------------------------------------------------------------------------
+# stout smearing (src/smearing)
+# ---------------------------------------------------------------------------
+class STOUT_Layer:
+    """Plaquette stout layer (stout_fast.jl:6-121): Ubar = exp(TA(C U^dag)) U."""
+
+    def __init__(self, loops="plaquette", rho=0.1, U=None):
+        names = [loops] if isinstance(loops, str) else list(loops)
+        if names != ["plaquette"]:
+            raise ValueError("the GB300 backend implements plaquette stout layers only")
+        rhos = [rho] if np.isscalar(rho) else list(rho)
+        if len(rhos) != 1:
+            raise ValueError("rho must be a scalar or have one entry per loop")
+        self.rho = float(rhos[0])
+
+
+class CovNeuralnet:
+    """Stack of smearing layers (Abstractsmearing.jl:61-99)."""
+
+    def __init__(self, U=None):
+        self.layers = []
+
+    def rhos(self):
+        return [l.rho for l in self.layers]
+
+    def __len__(self):
+        return len(self.layers)
+
+
+def stout_smearing(U, loops="plaquette", rho=0.1):
+    """stout_smearing(U; loops, rho) (src/API.jl:452-463): one plaquette layer."""
+    net = CovNeuralnet(U)
+    push_(net, STOUT_Layer(loops, rho, U))
+    return net
+
+
+class _StoutStack:
+    """A gf_stout workspace (levels, stored C, back-propagation buffers)."""
+
+    def __init__(self, ctx, rhos, precision="fp64", store=True):
+        if not 1 <= len(rhos) <= _lib.GF_MAX_STOUT:
+            raise ValueError("1..%d stout levels are supported" % _lib.GF_MAX_STOUT)
+        self.ctx = ctx
+        arr = (ctypes.c_double * len(rhos))(*rhos)
+        h = ctypes.c_void_p()
+        prec = _lib.GF_MIXED if precision == "mixed" else _lib.GF_FP64
+        call("gf_stout_create", ctx.h, len(rhos), arr, prec, 1 if store else 0, ctypes.byref(h), ctx=ctx.h)
+        self.h = h
+        self.precision = precision
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None) and _lib._lib is not None:
+                _lib._lib.gf_stout_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+SmearingResult = namedtuple("SmearingResult", ["configuration", "history", "derivative"])
+
+
+def calc_smearedU(U, smearing, calcdSdU=False, temps=None):
+    """Forward through every layer (Abstractsmearing.jl:237-272); the history
+    is the native stack that keeps each level for back_prop."""
+    stack = _StoutStack(U.ctx, smearing.rhos(), "fp64")
+    Uout = U.similar()
+    call("gf_stout_forward", U.ctx.h, stack.h, U.field.h, Uout.field.h, ctx=U.ctx.h)
+    return Uout, stack, None
+
+
+def smear(U, smearing, record=False, calcdSdU=False, temps=None):
+    """smear(U, smearing; record) (src/API.jl:472-480)."""
+    configuration, history, derivative = calc_smearedU(U, smearing, calcdSdU=calcdSdU, temps=temps)
+    return SmearingResult(configuration, history, derivative) if record else configuration
+
+
+def back_prop(dSdUbar, smearing, history, U):
+    """back_prop(δ, net, Uout_multi, U) (Abstractsmearing.jl:316-411): dS/dU on
+    the thin links from dS/dUbar (both general 3x3 fields, fp64)."""
+    out = Gaugefields4D(U.ctx, _lib.GF_MAT64)
+    call("gf_stout_backward", U.ctx.h, history.h, dSdUbar.field.h, out.field.h, ctx=U.ctx.h)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# gradient flow (src/smearing/gradientflow.jl)
+# ---------------------------------------------------------------------------
+class Gradientflow:
+    """Wilson flow with the Luescher RK3 integrator (gradientflow.jl:118-161)."""
+
+    def __init__(self, U, Nflow=1, eps=0.01):
+        self.Nflow = int(Nflow)
+        self.eps = float(eps)
+
+
+def gradient_flow(U, steps=1, step_size=0.01):
+    """gradient_flow(U; steps, step_size) (src/API.jl:420-437)."""
+    if steps <= 0:
+        raise ValueError("steps must be positive; got %d" % steps)
+    if step_size <= 0:
+        raise ValueError("step_size must be positive; got %s" % step_size)
+    return Gradientflow(U, Nflow=steps, eps=step_size)
+
+
+def flow_(U, g):
+    """flow!(U, g) (gradientflow.jl:171-238)."""
+    call("gf_flow", U.ctx.h, U.field.h, ctypes.c_double(g.eps), int(g.Nflow), ctx=U.ctx.h)
+    return U
+
+
+def add_force_(F, U, plaqonly=True, factor=1.0):
+    """add_force!(F, U; plaqonly=true, factor) (AbstractGaugefields.jl:2717-2763)."""
+    if not plaqonly:
+        raise ValueError("only plaqonly=true is implemented (the general branch of the reference is unused)")
+    call("gf_flow_force", U.ctx.h, U.field.h, F.field.h, ctypes.c_double(factor), ctx=U.ctx.h)
+    return F

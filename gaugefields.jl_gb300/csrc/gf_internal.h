@@ -1,0 +1,154 @@
+// Internal declarations shared by the translation units of libgfgb300.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <stdexcept>
+#include "lattice.cuh"
+#include "../../include/gaugefields_gb300.h"
+
+// Error carried from the CUDA layer to the C-ABI wrappers, which turn it into
+// a status code and keep the message for gf_last_error().
+struct gf_error : std::runtime_error {
+  int code;
+  gf_error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define GF_CUDA(call)                                                                    \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      throw gf_error(GF_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));     \
+  } while (0)
+
+namespace gf {
+// process-wide count of kernels launched by this library
+void count_launch();
+}
+#define GF_CHECK_LAUNCH()          \
+  do {                             \
+    gf::count_launch();            \
+    GF_CUDA(cudaGetLastError());   \
+  } while (0)
+
+#define GF_PROF_CAP 4096
+
+struct gf_field {
+  gf_ctx* ctx;
+  int kind;
+  void* ptr;
+  size_t bytes;
+  int owned;
+};
+
+struct gf_ctx {
+  int device;
+  gf::Geom geom;
+  cudaStream_t stream;
+  int own_stream;
+  std::string err;
+  // deterministic reductions: per-block partial sums and a pinned result slot
+  double* d_partials;
+  int partial_cap;
+  double* d_result;
+  double* h_result;
+  // work fields of the MD / flow drivers, allocated on first use
+  gf_field* w_link64;     // backup / W1 of the flow
+  gf_field* w_link64b;    // W2 of the flow
+  gf_field* w_mom[4];     // F0, F1, F2, Ftmp of the RK3 flow (fp64 coefficients)
+  gf_field* w_link32;     // fp32 12-real shadow of the thin links (mixed form)
+  gf_stout* w_stout64;    // stout workspace, fp64
+  gf_stout* w_stout32;    // stout workspace, fp32
+  int w_stout_nlev;
+  double w_stout_rho[GF_MAX_STOUT];
+  // per-kernel CUDA-event timing on the context's stream (gf_prof_*)
+  int prof_on;
+  int prof_n;
+  cudaEvent_t* prof_ev;  // 2 * GF_PROF_CAP events
+  int prof_kid[GF_PROF_CAP];
+  double prof_ms[GF_K_COUNT];
+  long long prof_cnt[GF_K_COUNT];
+};
+
+struct gf_stout {
+  gf_ctx* ctx;
+  int nlev;
+  double rho[GF_MAX_STOUT];
+  int precision;  // GF_FP64 or GF_FP32
+  int store;      // 1: keep C of every level from the forward pass
+  gf_field* lev_in[GF_MAX_STOUT + 1];  // lev_in[0] aliases the thin links
+  gf_field* C[GF_MAX_STOUT];
+  gf_field* Z;   // dS/dC of the level being pulled back
+  gf_field* Dp;  // local part of dS/dU (alpha term + (Y C)^dag)
+  gf_field* D[2];
+  int have_forward;
+};
+
+namespace gf {
+
+size_t field_bytes(const Geom& g, int kind);
+gf_field* field_new(gf_ctx* ctx, int kind);
+void field_delete(gf_field* f);
+
+inline int blocks_for(int n, int bs) { return (n + bs - 1) / bs; }
+
+// CUDA-event timing of one kernel launch (no-op unless gf_prof_enable is on)
+void prof_begin(gf_ctx* ctx, int kid);
+void prof_end(gf_ctx* ctx, int kid);
+void prof_flush(gf_ctx* ctx);
+struct ProfScope {
+  gf_ctx* c;
+  int k;
+  ProfScope(gf_ctx* c_, int k_) : c(c_), k(k_) { prof_begin(c, k); }
+  ~ProfScope() { prof_end(c, k); }
+};
+
+// ---- reductions (gf_fields.cu) ----
+// Deterministic two-stage sum of per-site doubles produced by a kernel that
+// writes one partial per block; returns the total on the host.
+double finish_reduction(gf_ctx* ctx, int nblocks);
+double kinetic(gf_ctx* ctx, const gf_field* P);
+
+// ---- field plumbing (gf_fields.cu) ----
+void upload_links(gf_ctx* ctx, gf_field* U, const double* host);
+void download_links(gf_ctx* ctx, const gf_field* U, double* host);
+void upload_mom(gf_ctx* ctx, gf_field* P, const double* host);
+void download_mom(gf_ctx* ctx, const gf_field* P, double* host);
+void cold_start(gf_ctx* ctx, gf_field* U);
+void hot_start(gf_ctx* ctx, gf_field* U, uint64_t seed);
+void gaussian_momenta(gf_ctx* ctx, gf_field* P, uint64_t seed, uint64_t sweep);
+void copy_field(gf_ctx* ctx, gf_field* dst, const gf_field* src);
+void zero_field(gf_ctx* ctx, gf_field* f);
+void mom_axpy(gf_ctx* ctx, gf_field* y, double a, const gf_field* x);  // y += a x
+void mom_scale(gf_ctx* ctx, gf_field* y, double a);                      // y *= a
+
+// ---- Wilson action pieces (gf_wilson.cu) ----
+double plaquette_sum(gf_ctx* ctx, const gf_field* U);  // sum_x sum_{mu<nu} Re tr P
+void staple_up(gf_ctx* ctx, const gf_field* U, int mu, gf_field* V);  // construct_staple! (mu field slot)
+// P <- keep * P + coef * TA-coefficients(U_mu * S_mu), S = sum of the six
+// staples (dS/dU order); keep = 0 overwrites P without reading it.
+void wilson_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double coef, double keep);
+
+// ---- link update (gf_update.cu) ----
+// U <- exp(i eps P) U, optional re-unitarisation, optional fp32 shadow copy.
+void link_update(gf_ctx* ctx, gf_field* U, const gf_field* P, double eps, int reunit, gf_field* shadow32);
+void exp_mom_links(gf_ctx* ctx, gf_field* W, const gf_field* P, double a, const gf_field* U);  // W = exp(i a P) U
+void reunitarize_links(gf_ctx* ctx, gf_field* U);
+void link64_to_32(gf_ctx* ctx, gf_field* dst, const gf_field* src);
+
+// ---- stout (gf_stout.cu) ----
+void stout_forward(gf_ctx* ctx, gf_stout* st, const gf_field* U, gf_field* Uout);
+// Pull dS/dUbar back to the thin links. If dSdUbar is null the top-level
+// derivative is taken from the Wilson action (coefficient beta/2 per staple)
+// on the smeared links. If P is non-null the thin-link result is turned into
+// the MD force and added as P += eps * F; otherwise it is written to dSdU.
+void stout_backward(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, double beta, gf_field* dSdU,
+                    gf_field* P, double eps);
+const gf_field* stout_top(const gf_stout* st);
+
+// ---- flow (gf_flow.cu) ----
+// F <- keep * F + factor * TA-coefficients(U_mu V_mu^dag), V = six-staple sum
+// (add_force!, plaqonly)
+void flow_force(gf_ctx* ctx, const gf_field* U, gf_field* F, double factor, double keep);
+
+}  // namespace gf

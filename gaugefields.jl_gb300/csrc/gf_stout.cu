@@ -1,0 +1,332 @@
+// Stout smearing (Morningstar-Peardon) forward and adjoint kernels.
+//
+// Forward, per level and link (forward!, src/smearing/stout_fast.jl:250-275):
+//   C_mu  = rho * sum_{nu != mu} [U_nu(x) U_mu(x+nu) U_nu(x+mu)^dag
+//                                 + U_nu(x-nu)^dag U_mu(x-nu) U_nu(x-nu+mu)] = rho S_mu^dag
+//   Omega = C_mu U_mu^dag,  Q = TA(Omega),  Ubar_mu = exp(Q) U_mu.
+//
+// Adjoint, per level (backward_dSdUαUβρ_add!, stout_fast.jl:317-408). With
+// Dbar = dS/dUbar (Wirtinger derivative, dS = 2 Re tr(dUbar Dbar)):
+//   Lambda = U Dbar, Gamma = C star dexp(Q)/dQ (CdexpQdQ!, stout_fast.jl:888-946)
+//   Y  = TA(Gamma)            (calc_dSdΩ!, :678-685)
+//   Z  = U^dag Y = dS/dC      (calc_dSdC!, :687)
+//   Dp = Dbar exp(Q) + (Y C)^dag   (calc_dSdu1! :629 and calc_dSdUdag! :692)
+//   D_nu(x) = Dp_nu(x) + rho * [pull-back of Z through C(U)]   (calc_dSdUν_fromdSCμ_add!, :712-785)
+// The last step is written as a gather over the 18 staple positions in which
+// a link U_nu(x) enters some C_kappa(y), so no atomics are needed.
+//
+// Two kernels per backward level: k_bwd_local (Lambda .. Dp, Z) and
+// k_bwd_gather (the pull-back through C, fused with the thin-link MD force
+// and momentum update at the bottom level).
+#include "gf_internal.h"
+#include "stencil.cuh"
+
+namespace gf {
+
+template <typename R>
+struct Prec;
+template <>
+struct Prec<double> {
+  typedef LinkSrc<double, false> Src;
+  typedef double2 LinkElem;
+  typedef double2 MatElem;
+  static constexpr int link_kind = GF_LINK64;
+  static constexpr int mat_kind = GF_MAT64;
+  static __device__ __forceinline__ void store_link(double2* p, int mu, int s, int V, const mat3<double>& m) {
+    LinkFull<double>::store(p, mu, s, V, m);
+  }
+};
+template <>
+struct Prec<float> {
+  typedef LinkSrc<float, true> Src;
+  typedef float4 LinkElem;
+  typedef float2 MatElem;
+  static constexpr int link_kind = GF_LINK32;
+  static constexpr int mat_kind = GF_MAT32;
+  static __device__ __forceinline__ void store_link(float4* p, int mu, int s, int V, const mat3<float>& m) {
+    Link12f::store(p, mu, s, V, m);
+  }
+};
+
+// i * r * A  (elementwise)
+template <typename R>
+__device__ __forceinline__ mat3<R> times_i(R r, const mat3<R>& a) {
+  mat3<R> b;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) b.e[i][j] = mk(-r * a.e[i][j].im, r * a.e[i][j].re);
+  return b;
+}
+
+// --------------------------------------------------------------------------
+// forward level
+// --------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(128)
+    k_stout_fwd(typename Prec<R>::Src U, typename Prec<R>::LinkElem* __restrict__ Uout,
+                typename Prec<R>::MatElem* __restrict__ Cout, Geom g, R rho) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  int mu = blockIdx.y;
+  if (s >= g.vol) return;
+  const int V = g.vol;
+  Site st = site_of(g, s);
+  mat3<R> S = staple_sum<R>(mu, U, g, st, s);
+  mat3<R> u = U(mu, s, V);
+  // Omega = rho (U S)^dag, Q = TA(Omega) = -rho TA(U S), exp(Q) = exp(i Qh), Qh = i rho TA(U S)
+  mat3<R> M = mul_nn(u, S);
+  mat3<R> qh = times_i(rho, ta_proj(M));
+  mat3<R> E = expiq(qh);
+  Prec<R>::store_link(Uout, mu, s, V, mul_nn(E, u));
+  if (Cout) LinkFull<R>::store(Cout, mu, s, V, scale(rho, dag(S)));
+}
+
+// --------------------------------------------------------------------------
+// backward, local part
+// --------------------------------------------------------------------------
+template <typename R, bool TOP>
+__global__ void __launch_bounds__(128)
+    k_bwd_local(typename Prec<R>::Src U, typename Prec<R>::Src Utop, const typename Prec<R>::MatElem* __restrict__ Dbar,
+                const typename Prec<R>::MatElem* __restrict__ Cst, typename Prec<R>::MatElem* __restrict__ Zout,
+                typename Prec<R>::MatElem* __restrict__ Dpout, Geom g, R rho, R halfbeta) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  int mu = blockIdx.y;
+  if (s >= g.vol) return;
+  const int V = g.vol;
+  Site st = site_of(g, s);
+  mat3<R> u = U(mu, s, V);
+  mat3<R> C;
+  if (Cst) C = LinkFull<R>::load(Cst, mu, s, V);
+  else C = scale(rho, dag(staple_sum<R>(mu, U, g, st, s)));
+  // Qh = -i TA(C U^dag)
+  mat3<R> qh = times_i(R(-1), ta_proj(mul_na(C, u)));
+  R c0, c1;
+  herm_invariants(qh, c0, c1);
+  ch_coef<R> cc;
+  ch_coefficients<R, true>(c0, c1, cc);
+  mat3<R> qh2 = mul_nn(qh, qh);
+  mat3<R> db;
+  if (TOP) db = scale(halfbeta, staple_sum<R>(mu, Utop, g, st, s));
+  else db = LinkFull<R>::load(Dbar, mu, s, V);
+  mat3<R> lam = mul_nn(u, db);
+  cplx<R> trL = trace(lam), trLQ = tr_nn(lam, qh), trLQ2 = tr_nn(lam, qh2);
+  cplx<R> trB1 = cc.b1[0] * trL + cc.b1[1] * trLQ + cc.b1[2] * trLQ2;
+  cplx<R> trB2 = cc.b2[0] * trL + cc.b2[1] * trLQ + cc.b2[2] * trLQ2;
+  // Gamma_MP = trB1 Qh + trB2 Qh^2 + f1 Lambda + f2 (Qh Lambda + Lambda Qh)
+  mat3<R> gam = mul_nn(qh, lam);
+  mac_nn(gam, lam, qh);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      cplx<R> v = cc.f[2] * gam.e[i][j];
+      fma_(v, cc.f[1], lam.e[i][j]);
+      fma_(v, trB1, qh.e[i][j]);
+      fma_(v, trB2, qh2.e[i][j]);
+      gam.e[i][j] = v;
+    }
+  // dS/dQ = -i Gamma_MP, Y = TA(dS/dQ)
+  mat3<R> Y = ta_proj(times_i(R(-1), gam));
+  LinkFull<R>::store(Zout, mu, s, V, mul_an(u, Y));
+  // exp(Q) = f0 + f1 Qh + f2 Qh^2
+  mat3<R> E;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      cplx<R> v = cc.f[1] * qh.e[i][j];
+      fma_(v, cc.f[2], qh2.e[i][j]);
+      if (i == j) v = v + cc.f[0];
+      E.e[i][j] = v;
+    }
+  mat3<R> dp = mul_nn(db, E);
+  mac_aa(dp, C, Y);  // (Y C)^dag = C^dag Y^dag
+  LinkFull<R>::store(Dpout, mu, s, V, dp);
+}
+
+// --------------------------------------------------------------------------
+// backward, gather of the pull-back through C(U)
+// --------------------------------------------------------------------------
+// Six contributions to D_nu(x) from the staples that involve the axis K:
+//  (a) U_K(x+nu) U_nu(x+K)^dag Z_K(x)          (b) U_K(x-K+nu)^dag U_nu(x-K)^dag Z_K(x-K)^dag
+//  (c) Z_K(x+nu)^dag U_nu(x+K)^dag U_K(x)^dag  (d) Z_K(x+nu-K) U_nu(x-K)^dag U_K(x-K)
+//  (e) U_K(x-K+nu)^dag Z_nu(x-K) U_K(x-K)      (f) U_K(x+nu) Z_nu(x+K) U_K(x)^dag
+template <typename R, int NU, int K>
+__device__ __forceinline__ void gather_axis(mat3<R>& acc, const typename Prec<R>::Src& U,
+                                            const typename Prec<R>::MatElem* __restrict__ Z, const Geom& g,
+                                            const Site& st, int s) {
+  const int V = g.vol;
+  const int xpn = nbr<NU>(g, st, +1);
+  const int xpk = nbr<K>(g, st, +1);
+  const int xmk = nbr<K>(g, st, -1);
+  const int xmk_pn = nbr2<K, NU>(g, st, -1, +1);
+  {
+    mat3<R> a1 = U(K, xpn, V);   // U_K(x+nu)
+    mat3<R> a2 = U(NU, xpk, V);  // U_nu(x+K)
+    mat3<R> t = mul_na(a1, a2);
+    mac_nn(acc, t, LinkFull<R>::load(Z, K, s, V));  // (a)
+    mat3<R> a6 = U(K, s, V);  // U_K(x)
+    t = mul_nn(a1, LinkFull<R>::load(Z, NU, xpk, V));
+    mac_na(acc, t, a6);  // (f)
+    t = mul_nn(a6, a2);
+    mac_aa(acc, LinkFull<R>::load(Z, K, xpn, V), t);  // (c)
+  }
+  {
+    mat3<R> a3 = U(K, xmk_pn, V);  // U_K(x-K+nu)
+    mat3<R> a4 = U(NU, xmk, V);    // U_nu(x-K)
+    mat3<R> a5 = U(K, xmk, V);     // U_K(x-K)
+    mat3<R> t = mul_nn(a4, a3);
+    mac_aa(acc, t, LinkFull<R>::load(Z, K, xmk, V));  // (b)
+    t = mul_na(LinkFull<R>::load(Z, K, xmk_pn, V), a4);
+    mac_nn(acc, t, a5);  // (d)
+    t = mul_an(a3, LinkFull<R>::load(Z, NU, xmk, V));
+    mac_nn(acc, t, a5);  // (e)
+  }
+}
+
+template <typename R, int NU>
+__device__ __forceinline__ mat3<R> gather_all(const typename Prec<R>::Src& U,
+                                              const typename Prec<R>::MatElem* __restrict__ Z, const Geom& g,
+                                              const Site& st, int s) {
+  mat3<R> acc = zero3<R>();
+  if constexpr (NU != 0) gather_axis<R, NU, 0>(acc, U, Z, g, st, s);
+  if constexpr (NU != 1) gather_axis<R, NU, 1>(acc, U, Z, g, st, s);
+  if constexpr (NU != 2) gather_axis<R, NU, 2>(acc, U, Z, g, st, s);
+  if constexpr (NU != 3) gather_axis<R, NU, 3>(acc, U, Z, g, st, s);
+  return acc;
+}
+
+template <typename R, bool FORCE>
+__global__ void __launch_bounds__(128)
+    k_bwd_gather(typename Prec<R>::Src U, const typename Prec<R>::MatElem* __restrict__ Z,
+                 const typename Prec<R>::MatElem* __restrict__ Dp, typename Prec<R>::MatElem* __restrict__ Dout,
+                 double* __restrict__ P, Geom g, R rho, double coef) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  int nu = blockIdx.y;
+  if (s >= g.vol) return;
+  const int V = g.vol;
+  Site st = site_of(g, s);
+  mat3<R> acc;
+  switch (nu) {
+    case 0: acc = gather_all<R, 0>(U, Z, g, st, s); break;
+    case 1: acc = gather_all<R, 1>(U, Z, g, st, s); break;
+    case 2: acc = gather_all<R, 2>(U, Z, g, st, s); break;
+    default: acc = gather_all<R, 3>(U, Z, g, st, s); break;
+  }
+  mat3<R> d = LinkFull<R>::load(Dp, nu, s, V);
+  axpy_to(d, rho, acc);
+  if (FORCE) {
+    // thin-link MD force F = -(1/3) TA(U dS/dU), P += eps F  (coef = -eps/3)
+    mat3<R> M = mul_nn(U(nu, s, V), d);
+    R c[8];
+    ta_coeffs(M, c);
+    double* p = P + (size_t)nu * 8 * V + s;
+#pragma unroll
+    for (int a = 0; a < 8; ++a) p[(size_t)a * V] += coef * (double)c[a];
+  } else {
+    LinkFull<R>::store(Dout, nu, s, V, d);
+  }
+}
+
+// --------------------------------------------------------------------------
+// host drivers
+// --------------------------------------------------------------------------
+template <typename R>
+static typename Prec<R>::Src src_of(const gf_field* f) {
+  typename Prec<R>::Src s;
+  s.p = (const typename Prec<R>::LinkElem*)f->ptr;
+  return s;
+}
+
+template <typename R>
+static void forward_impl(gf_ctx* ctx, gf_stout* st) {
+  dim3 grid(blocks_for(ctx->geom.vol, 128), 4);
+  for (int l = 0; l < st->nlev; ++l) {
+    ProfScope prof(ctx, GF_K_STOUT_FWD);
+    k_stout_fwd<R><<<grid, 128, 0, ctx->stream>>>(
+        src_of<R>(st->lev_in[l]), (typename Prec<R>::LinkElem*)st->lev_in[l + 1]->ptr,
+        st->store ? (typename Prec<R>::MatElem*)st->C[l]->ptr : nullptr, ctx->geom, (R)st->rho[l]);
+    GF_CHECK_LAUNCH();
+  }
+}
+
+void stout_forward(gf_ctx* ctx, gf_stout* st, const gf_field* U, gf_field* Uout) {
+  int lk = st->precision == GF_FP64 ? GF_LINK64 : GF_LINK32;
+  gf_field* old = st->lev_in[0];
+  if (U->kind == lk) {
+    // alias the caller's thin links (not owned by the stack)
+    gf_field* a = new gf_field(*U);
+    a->owned = 0;
+    st->lev_in[0] = a;
+    field_delete(old);  // frees storage only if the old entry was owned
+  } else if (st->precision != GF_FP64 && U->kind == GF_LINK64) {
+    // mixed stack fed with fp64 links: keep an owned fp32 12-real thin copy
+    if (!old || !old->owned) {
+      st->lev_in[0] = field_new(ctx, GF_LINK32);
+      field_delete(old);
+    }
+    copy_field(ctx, st->lev_in[0], U);
+  } else {
+    throw gf_error(GF_EINVAL, "stout forward: link field kind does not match the stack precision");
+  }
+  if (st->precision == GF_FP64) forward_impl<double>(ctx, st);
+  else forward_impl<float>(ctx, st);
+  st->have_forward = 1;
+  if (Uout) copy_field(ctx, Uout, st->lev_in[st->nlev]);
+}
+
+const gf_field* stout_top(const gf_stout* st) { return st->lev_in[st->nlev]; }
+
+template <typename R>
+static void backward_impl(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, double beta, gf_field* dSdU,
+                          gf_field* P, double eps) {
+  dim3 grid(blocks_for(ctx->geom.vol, 128), 4);
+  typedef typename Prec<R>::MatElem ME;
+  const ME* dbar = dSdUbar ? (const ME*)dSdUbar->ptr : nullptr;
+  int cur = 0;
+  for (int l = st->nlev - 1; l >= 0; --l) {
+    bool top = (l == st->nlev - 1) && dSdUbar == nullptr;
+    const ME* Cst = st->store ? (const ME*)st->C[l]->ptr : nullptr;
+    const ME* din = (l == st->nlev - 1) ? dbar : (const ME*)st->D[cur]->ptr;
+    {
+    ProfScope prof(ctx, GF_K_BWD_LOCAL);
+    if (top) {
+      k_bwd_local<R, true><<<grid, 128, 0, ctx->stream>>>(src_of<R>(st->lev_in[l]), src_of<R>(st->lev_in[l + 1]),
+                                                          nullptr, Cst, (ME*)st->Z->ptr, (ME*)st->Dp->ptr, ctx->geom,
+                                                          (R)st->rho[l], (R)(0.5 * beta));
+    } else {
+      k_bwd_local<R, false><<<grid, 128, 0, ctx->stream>>>(src_of<R>(st->lev_in[l]), src_of<R>(st->lev_in[l + 1]),
+                                                           din, Cst, (ME*)st->Z->ptr, (ME*)st->Dp->ptr, ctx->geom,
+                                                           (R)st->rho[l], (R)(0.5 * beta));
+    }
+    GF_CHECK_LAUNCH();
+    }
+    int nxt = cur ^ 1;
+    ProfScope prof(ctx, GF_K_BWD_GATHER);
+    if (l == 0 && P) {
+      k_bwd_gather<R, true><<<grid, 128, 0, ctx->stream>>>(src_of<R>(st->lev_in[0]), (const ME*)st->Z->ptr,
+                                                           (const ME*)st->Dp->ptr, nullptr, (double*)P->ptr,
+                                                           ctx->geom, (R)st->rho[0], -eps / 3.0);
+    } else {
+      ME* out = (l == 0) ? (ME*)dSdU->ptr : (ME*)st->D[nxt]->ptr;
+      k_bwd_gather<R, false><<<grid, 128, 0, ctx->stream>>>(src_of<R>(st->lev_in[l]), (const ME*)st->Z->ptr,
+                                                            (const ME*)st->Dp->ptr, out, nullptr, ctx->geom,
+                                                            (R)st->rho[l], 0.0);
+    }
+    GF_CHECK_LAUNCH();
+    cur = nxt;
+  }
+}
+
+void stout_backward(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, double beta, gf_field* dSdU, gf_field* P,
+                    double eps) {
+  if (!st->have_forward) throw gf_error(GF_ESTATE, "stout backward called before forward");
+  if (st->nlev < 1) throw gf_error(GF_EINVAL, "stout backward needs at least one level");
+  int mk = st->precision == GF_FP64 ? GF_MAT64 : GF_MAT32;
+  if (dSdUbar && dSdUbar->kind != mk) throw gf_error(GF_EINVAL, "stout backward: dS/dUbar kind does not match the stack precision");
+  if (!P && (!dSdU || dSdU->kind != mk)) throw gf_error(GF_EINVAL, "stout backward: dS/dU kind does not match the stack precision");
+  if (st->precision == GF_FP64) backward_impl<double>(ctx, st, dSdUbar, beta, dSdU, P, eps);
+  else backward_impl<float>(ctx, st, dSdUbar, beta, dSdU, P, eps);
+}
+
+}  // namespace gf

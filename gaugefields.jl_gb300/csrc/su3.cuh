@@ -1,0 +1,420 @@
+// SU(3) / 3x3 complex matrix arithmetic shared by every kernel of the
+// library. Templated on the real type (float for the mixed-precision force
+// path, double for the plain FP64 path and for the Hamiltonian pieces).
+//
+// Conventions follow Gaugefields.jl:
+//  * link matrices are row-major 3x3 complex (element (i,j) = row i, column j);
+//  * the su(3) coefficient map of a matrix M is the one of
+//    Traceless_antihermitian_add! (src/4D/TA_gaugefields_4D_serial.jl:181-269):
+//    TA(M) = (M - M^dag)/2 - tr(M - M^dag)/6 = i * sum_a c_a lambda_a / 2;
+//  * momenta P = sum_a p_a lambda_a / 2 are Hermitian and the link update is
+//    U <- exp(i eps P) U (exptU! of src/4D/TA_gaugefields_4D_serial.jl:760).
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+
+#define GF_HD __host__ __device__ __forceinline__
+
+namespace gf {
+
+template <typename R>
+struct cplx {
+  R re, im;
+};
+
+template <typename R>
+GF_HD cplx<R> mk(R re, R im) {
+  cplx<R> c;
+  c.re = re;
+  c.im = im;
+  return c;
+}
+template <typename R>
+GF_HD cplx<R> operator+(cplx<R> a, cplx<R> b) { return mk(a.re + b.re, a.im + b.im); }
+template <typename R>
+GF_HD cplx<R> operator-(cplx<R> a, cplx<R> b) { return mk(a.re - b.re, a.im - b.im); }
+template <typename R>
+GF_HD cplx<R> operator*(cplx<R> a, cplx<R> b) {
+  return mk(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+template <typename R>
+GF_HD cplx<R> operator*(R s, cplx<R> a) { return mk(s * a.re, s * a.im); }
+template <typename R>
+GF_HD cplx<R> conj(cplx<R> a) { return mk(a.re, -a.im); }
+// a * conj(b)
+template <typename R>
+GF_HD cplx<R> mulc(cplx<R> a, cplx<R> b) {
+  return mk(a.re * b.re + a.im * b.im, a.im * b.re - a.re * b.im);
+}
+// conj(a) * conj(b)
+template <typename R>
+GF_HD cplx<R> cmulc(cplx<R> a, cplx<R> b) {
+  return mk(a.re * b.re - a.im * b.im, -(a.re * b.im + a.im * b.re));
+}
+// c += a*b
+template <typename R>
+GF_HD void fma_(cplx<R>& c, cplx<R> a, cplx<R> b) {
+  c.re += a.re * b.re - a.im * b.im;
+  c.im += a.re * b.im + a.im * b.re;
+}
+
+template <typename R>
+struct mat3 {
+  cplx<R> e[3][3];
+};
+
+template <typename R>
+GF_HD mat3<R> zero3() {
+  mat3<R> m;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) m.e[i][j] = mk<R>(0, 0);
+  return m;
+}
+template <typename R>
+GF_HD mat3<R> ident3() {
+  mat3<R> m = zero3<R>();
+  m.e[0][0].re = m.e[1][1].re = m.e[2][2].re = R(1);
+  return m;
+}
+
+// A*B
+template <typename R>
+GF_HD mat3<R> mul_nn(const mat3<R>& a, const mat3<R>& b) {
+  mat3<R> c;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      cplx<R> s = a.e[i][0] * b.e[0][j];
+      fma_(s, a.e[i][1], b.e[1][j]);
+      fma_(s, a.e[i][2], b.e[2][j]);
+      c.e[i][j] = s;
+    }
+  return c;
+}
+// A*B^dag
+template <typename R>
+GF_HD mat3<R> mul_na(const mat3<R>& a, const mat3<R>& b) {
+  mat3<R> c;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      cplx<R> s = mulc(a.e[i][0], b.e[j][0]);
+      s = s + mulc(a.e[i][1], b.e[j][1]);
+      s = s + mulc(a.e[i][2], b.e[j][2]);
+      c.e[i][j] = s;
+    }
+  return c;
+}
+// A^dag*B
+template <typename R>
+GF_HD mat3<R> mul_an(const mat3<R>& a, const mat3<R>& b) {
+  mat3<R> c;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      cplx<R> s = conj(a.e[0][i]) * b.e[0][j];
+      fma_(s, conj(a.e[1][i]), b.e[1][j]);
+      fma_(s, conj(a.e[2][i]), b.e[2][j]);
+      c.e[i][j] = s;
+    }
+  return c;
+}
+// A^dag*B^dag
+template <typename R>
+GF_HD mat3<R> mul_aa(const mat3<R>& a, const mat3<R>& b) {
+  mat3<R> c;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      cplx<R> s = cmulc(a.e[0][i], b.e[j][0]);
+      s = s + cmulc(a.e[1][i], b.e[j][1]);
+      s = s + cmulc(a.e[2][i], b.e[j][2]);
+      c.e[i][j] = s;
+    }
+  return c;
+}
+template <typename R>
+GF_HD mat3<R> dag(const mat3<R>& a) {
+  mat3<R> c;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) c.e[i][j] = conj(a.e[j][i]);
+  return c;
+}
+template <typename R>
+GF_HD void add_to(mat3<R>& c, const mat3<R>& a) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) c.e[i][j] = c.e[i][j] + a.e[i][j];
+}
+// c += s*a
+template <typename R>
+GF_HD void axpy_to(mat3<R>& c, R s, const mat3<R>& a) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      c.e[i][j].re += s * a.e[i][j].re;
+      c.e[i][j].im += s * a.e[i][j].im;
+    }
+}
+template <typename R>
+GF_HD mat3<R> scale(R s, const mat3<R>& a) {
+  mat3<R> c;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) c.e[i][j] = s * a.e[i][j];
+  return c;
+}
+template <typename R>
+GF_HD cplx<R> trace(const mat3<R>& a) {
+  return a.e[0][0] + a.e[1][1] + a.e[2][2];
+}
+// Re tr(A B^dag) = sum_ij Re(A_ij conj(B_ij))
+template <typename R>
+GF_HD R retr_na(const mat3<R>& a, const mat3<R>& b) {
+  R s = R(0);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) s += a.e[i][j].re * b.e[i][j].re + a.e[i][j].im * b.e[i][j].im;
+  return s;
+}
+// tr(A B)
+template <typename R>
+GF_HD cplx<R> tr_nn(const mat3<R>& a, const mat3<R>& b) {
+  cplx<R> s = mk<R>(0, 0);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) fma_(s, a.e[i][k], b.e[k][i]);
+  return s;
+}
+
+// Traceless anti-Hermitian projection as a matrix:
+// TA(M) = (M - M^dag)/2 - tr(M - M^dag)/6 * 1.
+template <typename R>
+GF_HD mat3<R> ta_proj(const mat3<R>& m) {
+  mat3<R> y;
+  R tri = (m.e[0][0].im + m.e[1][1].im + m.e[2][2].im) * (R(1) / R(3));
+#pragma unroll
+  for (int i = 0; i < 3; ++i) y.e[i][i] = mk<R>(R(0), m.e[i][i].im - tri);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = i + 1; j < 3; ++j) {
+      cplx<R> x = m.e[i][j] - conj(m.e[j][i]);
+      y.e[i][j] = R(0.5) * x;
+      y.e[j][i] = mk<R>(R(-0.5) * x.re, R(0.5) * x.im);
+    }
+  return y;
+}
+
+// su(3) coefficients c_a (a = 1..8 stored 0..7) of TA(M), with
+// TA(M) = i sum_a c_a lambda_a / 2. This is the coefficient map of
+// Traceless_antihermitian_add! for NC = 3.
+template <typename R>
+GF_HD void ta_coeffs(const mat3<R>& m, R c[8]) {
+  const R sr3i = R(0.57735026918962576451);  // 1/sqrt(3)
+  // off-diagonal: x_ij = M_ij - conj(M_ji) = 2 y_ij
+  cplx<R> x12 = m.e[0][1] - conj(m.e[1][0]);
+  cplx<R> x13 = m.e[0][2] - conj(m.e[2][0]);
+  cplx<R> x23 = m.e[1][2] - conj(m.e[2][1]);
+  c[0] = x12.im;
+  c[1] = x12.re;
+  c[3] = x13.im;
+  c[4] = x13.re;
+  c[5] = x23.im;
+  c[6] = x23.re;
+  R d1 = m.e[0][0].im, d2 = m.e[1][1].im, d3 = m.e[2][2].im;
+  c[2] = d1 - d2;
+  c[7] = sr3i * (d1 + d2 - R(2) * d3);
+}
+
+// Hermitian matrix Q = sum_a p_a lambda_a / 2 (Gell-Mann basis).
+template <typename R>
+GF_HD mat3<R> herm_from_coeffs(const R p[8]) {
+  const R sr3i = R(0.57735026918962576451);
+  mat3<R> q;
+  R h = R(0.5);
+  q.e[0][0] = mk<R>(h * (p[2] + sr3i * p[7]), R(0));
+  q.e[1][1] = mk<R>(h * (-p[2] + sr3i * p[7]), R(0));
+  q.e[2][2] = mk<R>(-h * R(2) * sr3i * p[7], R(0));
+  q.e[0][1] = mk<R>(h * p[0], -h * p[1]);
+  q.e[1][0] = mk<R>(h * p[0], h * p[1]);
+  q.e[0][2] = mk<R>(h * p[3], -h * p[4]);
+  q.e[2][0] = mk<R>(h * p[3], h * p[4]);
+  q.e[1][2] = mk<R>(h * p[5], -h * p[6]);
+  q.e[2][1] = mk<R>(h * p[5], h * p[6]);
+  return q;
+}
+
+// Third row of an SU(3) matrix from its first two rows: row3 = conj(row1 x row2)
+// (m3complv3! of src/AbstractGaugefields.jl:3431).
+template <typename R>
+GF_HD void reconstruct_row3(mat3<R>& u) {
+  u.e[2][0] = conj(u.e[0][1] * u.e[1][2] - u.e[0][2] * u.e[1][1]);
+  u.e[2][1] = conj(u.e[0][2] * u.e[1][0] - u.e[0][0] * u.e[1][2]);
+  u.e[2][2] = conj(u.e[0][0] * u.e[1][1] - u.e[0][1] * u.e[1][0]);
+}
+
+// Re-unitarisation: Gram-Schmidt of rows 1-2, row 3 from the cross product
+// (normalize3! of src/AbstractGaugefields.jl:3378-3429).
+template <typename R>
+GF_HD void reunitarize(mat3<R>& u) {
+  R n1 = R(0);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) n1 += u.e[0][j].re * u.e[0][j].re + u.e[0][j].im * u.e[0][j].im;
+  // w = <row1, row2> = sum_j u2j conj(u1j)
+  cplx<R> w = mk<R>(0, 0);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) w = w + mulc(u.e[1][j], u.e[0][j]);
+  R inv1 = R(1) / n1;
+  w = mk<R>(-w.re * inv1, -w.im * inv1);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) fma_(u.e[1][j], w, u.e[0][j]);
+  R n2 = R(0);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) n2 += u.e[1][j].re * u.e[1][j].re + u.e[1][j].im * u.e[1][j].im;
+  R s1 = R(1) / sqrt(n1), s2 = R(1) / sqrt(n2);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    u.e[0][j] = s1 * u.e[0][j];
+    u.e[1][j] = s2 * u.e[1][j];
+  }
+  reconstruct_row3(u);
+}
+
+// ---------------------------------------------------------------------------
+// Cayley-Hamilton exponential of i*Q for a traceless Hermitian 3x3 Q:
+//   exp(iQ) = f0 + f1 Q + f2 Q^2,
+// with c0 = det Q, c1 = tr(Q^2)/2 and Q^3 = c1 Q + c0 (Cayley-Hamilton).
+// The coefficients f_j(c0, c1) and their derivatives b1_j = df_j/dc1,
+// b2_j = df_j/dc0 (the B1, B2 matrices of the stout derivative,
+// calc_coefficients_Q in src/AbstractGaugefields.jl:3284) are summed from the
+// power series exp(iQ) = sum_n (iQ)^n/n!, with every power reduced to
+// a_n + b_n Q + c_n Q^2 by the recursion
+//   a_{n+1} = c0 c_n,  b_{n+1} = a_n + c1 c_n,  c_{n+1} = b_n .
+// The series is stable for the small |Q| of link updates, flow steps and
+// stout layers (no division by (9u^2 - w^2)^2 as in the closed form), and it
+// is summed until the term falls below the working precision.
+// ---------------------------------------------------------------------------
+template <typename R>
+struct ch_coef {
+  cplx<R> f[3];
+  cplx<R> b1[3];  // d f_j / d c1
+  cplx<R> b2[3];  // d f_j / d c0
+};
+
+template <typename R>
+GF_HD R ch_eps();
+template <>
+GF_HD float ch_eps<float>() { return 3.0e-8f; }
+template <>
+GF_HD double ch_eps<double>() { return 5.0e-18; }
+
+template <typename R, bool DERIV>
+GF_HD void ch_coefficients(R c0, R c1, ch_coef<R>& out) {
+  // power coefficients of Q^n and their partial derivatives
+  R a = R(1), b = R(0), c = R(0);
+  R a0 = 0, b0 = 0, c0d = 0;  // d/dc0
+  R a1 = 0, b1 = 0, c1d = 0;  // d/dc1
+  // running 1/n! and phase i^n (as index n mod 4)
+  R fr[3] = {R(1), R(0), R(0)}, fi[3] = {R(0), R(0), R(0)};
+  R d1r[3] = {0, 0, 0}, d1i[3] = {0, 0, 0}, d2r[3] = {0, 0, 0}, d2i[3] = {0, 0, 0};
+  R fact = R(1);
+  // bound of |Q^n| coefficient magnitude used for the stopping rule
+  for (int n = 1; n < 64; ++n) {
+    // advance powers: Q^n from Q^{n-1}
+    R na = c0 * c;
+    R nb = a + c1 * c;
+    R nc = b;
+    R na0 = c + c0 * c0d;
+    R nb0 = a0 + c1 * c0d;
+    R nc0 = b0;
+    R na1 = c0 * c1d;
+    R nb1 = a1 + c + c1 * c1d;
+    R nc1 = b1;
+    a = na; b = nb; c = nc;
+    a0 = na0; b0 = nb0; c0d = nc0;
+    a1 = na1; b1 = nb1; c1d = nc1;
+    fact = fact / R(n);
+    R ta = a * fact, tb = b * fact, tc = c * fact;
+    // i^n: n%4 = 0 -> 1, 1 -> i, 2 -> -1, 3 -> -i
+    int ph = n & 3;
+    R sr = (ph == 0) ? R(1) : ((ph == 2) ? R(-1) : R(0));
+    R si = (ph == 1) ? R(1) : ((ph == 3) ? R(-1) : R(0));
+    fr[0] += sr * ta; fi[0] += si * ta;
+    fr[1] += sr * tb; fi[1] += si * tb;
+    fr[2] += sr * tc; fi[2] += si * tc;
+    R mag = fabs(ta) + fabs(tb) + fabs(tc);
+    if (DERIV) {
+      R ta0 = a0 * fact, tb0 = b0 * fact, tc0 = c0d * fact;
+      R ta1 = a1 * fact, tb1 = b1 * fact, tc1 = c1d * fact;
+      d2r[0] += sr * ta0; d2i[0] += si * ta0;
+      d2r[1] += sr * tb0; d2i[1] += si * tb0;
+      d2r[2] += sr * tc0; d2i[2] += si * tc0;
+      d1r[0] += sr * ta1; d1i[0] += si * ta1;
+      d1r[1] += sr * tb1; d1i[1] += si * tb1;
+      d1r[2] += sr * tc1; d1i[2] += si * tc1;
+      mag += fabs(ta0) + fabs(tb0) + fabs(tc0) + fabs(ta1) + fabs(tb1) + fabs(tc1);
+    }
+    if (n >= 4 && mag < ch_eps<R>()) break;
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    out.f[j] = mk(fr[j], fi[j]);
+    if (DERIV) {
+      out.b1[j] = mk(d1r[j], d1i[j]);
+      out.b2[j] = mk(d2r[j], d2i[j]);
+    }
+  }
+}
+
+// c1 = tr(Q^2)/2 and c0 = det(Q) of a traceless Hermitian matrix.
+template <typename R>
+GF_HD void herm_invariants(const mat3<R>& q, R& c0, R& c1) {
+  R q11 = q.e[0][0].re, q22 = q.e[1][1].re, q33 = q.e[2][2].re;
+  cplx<R> q12 = q.e[0][1], q13 = q.e[0][2], q23 = q.e[1][2];
+  R a12 = q12.re * q12.re + q12.im * q12.im;
+  R a13 = q13.re * q13.re + q13.im * q13.im;
+  R a23 = q23.re * q23.re + q23.im * q23.im;
+  c1 = R(0.5) * (q11 * q11 + q22 * q22 + q33 * q33) + a12 + a13 + a23;
+  // det = q11 q22 q33 + 2 Re(q12 q23 q31) - q11|q23|^2 - q22|q13|^2 - q33|q12|^2
+  cplx<R> t = q12 * q23;
+  R re3 = t.re * q13.re + t.im * q13.im;  // Re(q12 q23 conj(q13))
+  c0 = q11 * q22 * q33 + R(2) * re3 - q11 * a23 - q22 * a13 - q33 * a12;
+}
+
+// exp(iQ) for traceless Hermitian Q. Q2 receives Q^2 (callers reuse it).
+template <typename R>
+GF_HD mat3<R> expiq(const mat3<R>& q, mat3<R>* q2out = nullptr) {
+  R c0, c1;
+  herm_invariants(q, c0, c1);
+  ch_coef<R> cc;
+  ch_coefficients<R, false>(c0, c1, cc);
+  mat3<R> q2 = mul_nn(q, q);
+  mat3<R> e;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      cplx<R> v = cc.f[1] * q.e[i][j];
+      fma_(v, cc.f[2], q2.e[i][j]);
+      if (i == j) v = v + cc.f[0];
+      e.e[i][j] = v;
+    }
+  if (q2out) *q2out = q2;
+  return e;
+}
+
+}  // namespace gf

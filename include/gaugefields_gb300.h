@@ -1,0 +1,211 @@
+/*
+ * gaugefields_gb300.h -- C-ABI of libgfgb300.so, the GB300 (sm_103a) backend
+ * for the SU(3) gauge-link hot path of Gaugefields.jl.
+ *
+ * Every entry point returns an int status (GF_OK = 0, negative on error) and
+ * never lets a C++ exception cross the ABI; gf_last_error() returns the text
+ * of the last failure on a context. Plain pointers and sizes only.
+ *
+ * Host arrays use the reference's layouts:
+ *   links   : complex128 (3,3,NX,NY,NZ,NT) column-major per direction, the four
+ *             directions contiguous (Gaugefields_4D_nowing.U, or the
+ *             LatticeMatrix interior of Gaugefields_4D_MPILattice without halo)
+ *             -> 4*9*V complex = 72*V doubles (re,im interleaved)
+ *   momenta : Float64 (8,NX,NY,NZ,NT) per direction, contiguous over the four
+ *             directions (TA_Gaugefields_4D_serial.a) -> 32*V doubles
+ * Device storage is the library's own (even/odd site-major SoA) and is opaque.
+ *
+ * Reference citations are paths inside the Gaugefields.jl source tree.
+ */
+#ifndef GAUGEFIELDS_GB300_H
+#define GAUGEFIELDS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define GF_OK 0
+#define GF_EINVAL (-1)  /* bad argument: ArgumentError in the reference */
+#define GF_ENOMEM (-2)  /* device allocation failed */
+#define GF_ECUDA (-3)   /* CUDA runtime error */
+#define GF_ENAN (-4)    /* non-finite value detected (e.g. Delta H) */
+#define GF_ESTATE (-5)  /* call out of order (e.g. backward before forward) */
+
+/* field kinds */
+#define GF_LINK64 1 /* SU(3) links, complex128, 18 reals per link */
+#define GF_LINK32 2 /* SU(3) links, fp32 two-row 12-real storage */
+#define GF_MOM64 3  /* su(3) momenta / forces, 8 fp64 coefficients per link */
+#define GF_MAT64 4  /* general 3x3 complex per link, fp64 (dS/dU, staples) */
+#define GF_MAT32 5  /* general 3x3 complex per link, fp32 */
+
+/* precision of the force / stout path */
+#define GF_FP64 0  /* plain form: fp64 throughout */
+#define GF_MIXED 1 /* fp32 force and stout (12-real links), fp64 H / updates */
+
+/* integrators of the MD driver (molecular_dynamics.jl:604-616) */
+#define GF_QPQ 0
+#define GF_PQP 1
+
+#define GF_MAX_STOUT 4
+
+typedef struct gf_ctx gf_ctx;
+typedef struct gf_field gf_field;
+typedef struct gf_stout gf_stout;
+
+/* MD parameters: md_driver(U, action; steps, trajectory_length, integrator)
+ * (src/molecular_dynamics.jl:440-483) with the Wilson GaugeAction
+ * push!(action, beta/2, plaq U plaq^dag) and an optional stout stack
+ * (STOUT_Layer, src/smearing/stout_fast.jl:6-121). */
+typedef struct gf_md_params {
+  double beta;           /* Wilson coupling */
+  double tau;            /* trajectory_length, finite and nonzero */
+  int steps;             /* > 0 */
+  int integrator;        /* GF_QPQ or GF_PQP */
+  int precision;         /* GF_FP64 or GF_MIXED */
+  int nstout;            /* 0 .. GF_MAX_STOUT smearing levels */
+  double rho[GF_MAX_STOUT];
+  int reunitarize;       /* re-unitarise links after every link update */
+} gf_md_params;
+
+/* ---- context ------------------------------------------------------------ */
+/* Replaces the lattice/PE bookkeeping of Gaugefields_4D_MPILattice
+ * (src/4D/mpi_jacc/gaugefields_4D_MPILattice.jl:34-121). L = {NX,NY,NZ,NT};
+ * NX must be even (even/odd site order); one CUDA device per context. */
+int gf_ctx_create(const int L[4], int device, gf_ctx** out);
+int gf_ctx_destroy(gf_ctx* ctx);
+/* Run all work of the context on a caller-owned cudaStream_t (NULL restores
+ * the context's own stream). */
+int gf_ctx_set_stream(gf_ctx* ctx, void* cuda_stream);
+int gf_ctx_synchronize(gf_ctx* ctx);
+const char* gf_last_error(const gf_ctx* ctx);
+int gf_ctx_volume(const gf_ctx* ctx, int64_t* out);
+
+/* ---- fields ------------------------------------------------------------- */
+/* similar(U[1]) / initialize_TA_Gaugefields(U) (AbstractGaugefields.jl,
+ * TA_Gaugefields.jl:140-160): allocate a device field of the given kind. */
+int gf_field_alloc(gf_ctx* ctx, int kind, gf_field** out);
+int gf_field_free(gf_field* f);
+int gf_field_kind(const gf_field* f, int* kind);
+int gf_field_bytes(const gf_field* f, size_t* bytes);
+/* Device pointer of a field (for CUDA.jl / torch interop, library layout). */
+int gf_field_device_ptr(const gf_field* f, void** ptr);
+/* substitute_U! (gaugefields_4D_MPILattice.jl:509-611): dst <- src. LINK64 ->
+ * LINK32 converts to the fp32 12-real form; other kinds must match. */
+int gf_field_copy(gf_ctx* ctx, gf_field* dst, const gf_field* src);
+/* clear_U! */
+int gf_field_zero(gf_ctx* ctx, gf_field* f);
+
+/* ---- host transfer in the reference layout ----------------------------- */
+/* Upload/download link fields (LINK64 or MAT64) and momenta (MOM64); the
+ * round trip is exact. Replaces getindex/setindex!/substitute_U! host access
+ * (gaugefields_4D_MPILattice.jl:166-199) and the rank-0 gather of API.jl:531. */
+int gf_upload_links(gf_ctx* ctx, gf_field* U, const double* host);
+int gf_download_links(gf_ctx* ctx, const gf_field* U, double* host);
+int gf_upload_mom(gf_ctx* ctx, gf_field* P, const double* host);
+int gf_download_mom(gf_ctx* ctx, const gf_field* P, double* host);
+
+/* ---- starts and random fields ------------------------------------------ */
+/* gauge_configuration(L; start=:cold) (API.jl:178-251): all links = 1. */
+int gf_cold_start(gf_ctx* ctx, gf_field* U);
+/* gauge_configuration(L; start=:hot, seed): Haar-random SU(3) per link from a
+ * Gaussian 3x3 complex matrix (re, im ~ N(0,1/2)), Gram-Schmidt of the rows
+ * and the determinant phase divided out; counter-based Philox4x32-10 keyed by
+ * seed, so the start is independent of the launch shape. */
+int gf_hot_start(gf_ctx* ctx, gf_field* U, uint64_t seed);
+/* gaussian_momenta!(P; seed, sweep) (API.jl:341-368): p_a ~ N(0,1). */
+int gf_gaussian_momenta(gf_ctx* ctx, gf_field* P, uint64_t seed, uint64_t sweep);
+/* normalize_U! (AbstractGaugefields.jl:3378-3457) on every link. */
+int gf_reunitarize(gf_ctx* ctx, gf_field* U);
+
+/* ---- measurements ------------------------------------------------------- */
+/* calculate_Plaquette(U, temp, staple) (AbstractGaugefields.jl:2684-2699):
+ * sum_mu Re tr(U_mu V_mu^dag)/2 = sum_x sum_{mu<nu} Re tr P_munu(x).
+ * measure_plaquette divides by 6*V*3 (API.jl:395-404). Deterministic. */
+int gf_plaquette(gf_ctx* ctx, const gf_field* U, double* out);
+/* md_potential(::GaugeAction) (molecular_dynamics.jl:247) for the Wilson
+ * action beta/2 * (plaq U plaq^dag): -(beta/3) sum Re tr P. */
+int gf_action(gf_ctx* ctx, const gf_field* U, double beta, double* out);
+/* P*P (TA_gaugefields_4D_serial.jl:106-129): sum of p_a^2. */
+int gf_kinetic(gf_ctx* ctx, const gf_field* P, double* out);
+/* construct_staple!(V, U, mu, temp) (AbstractGaugefields.jl:2873-2923): the
+ * up staples sum_{nu != mu} U_nu(x) U_mu(x+nu) U_nu(x+mu)^dag into direction
+ * slot mu (0-based) of the MAT64/LINK64 field V. */
+int gf_staple(gf_ctx* ctx, const gf_field* U, int mu, gf_field* V);
+
+/* ---- molecular dynamics ------------------------------------------------- */
+/* md_force!(F, ::GaugeAction, U, ws) (molecular_dynamics.jl:251-267):
+ * F_mu = -(1/3) TA(U_mu dS/dU_mu), dS/dU_mu = beta/2 * sum of six staples. */
+int gf_force(gf_ctx* ctx, const gf_field* U, double beta, gf_field* F);
+/* update_momenta!(P, U, eps, driver) (molecular_dynamics.jl:539-551):
+ * P += eps * F(U), fused in one kernel. */
+int gf_mom_update(gf_ctx* ctx, gf_field* P, const gf_field* U, double eps, double beta);
+/* update_gaugefields!(U, P, eps, driver) (molecular_dynamics.jl:513-531):
+ * U_mu <- exp(i eps P_mu) U_mu (Cayley-Hamilton), reunit != 0 re-unitarises. */
+int gf_link_update(gf_ctx* ctx, gf_field* U, const gf_field* P, double eps, int reunit);
+/* md_hamiltonian (molecular_dynamics.jl:494-505): potential (on the smeared
+ * links when nstout > 0) + P*P/2, in fp64. */
+int gf_hamiltonian(gf_ctx* ctx, const gf_field* U, const gf_field* P, const gf_md_params* prm, double* out);
+/* md_trajectory!(U, P, driver) (molecular_dynamics.jl:712-730): one QPQ/PQP
+ * trajectory. out[0..2] = initial H, final H, Delta H. prm->precision selects
+ * the plain fp64 or the mixed form. */
+int gf_md_trajectory(gf_ctx* ctx, gf_field* U, gf_field* P, const gf_md_params* prm, double out[3]);
+/* One HMC update of the application loop (docs/src/hmc.md:22-81): momenta
+ * refresh (seed, sweep), md_trajectory!, Metropolis test with the uniform
+ * `unif` in [0,1), rejection restores U. out = {H0, H1, dH, accepted}. */
+int gf_hmc_update(gf_ctx* ctx, gf_field* U, gf_field* P, const gf_md_params* prm, uint64_t seed,
+                  uint64_t sweep, double unif, double out[4]);
+
+/* ---- stout smearing ----------------------------------------------------- */
+/* STOUT_Layer stack (stout_fast.jl:6-121) / CovNeuralnet of nlev plaquette
+ * layers with coefficients rho[0..nlev-1]. precision GF_FP64 or GF_MIXED
+ * (fp32 12-real links); store != 0 keeps C_mu of every level from the
+ * forward pass, store == 0 recomputes it in the backward pass. */
+int gf_stout_create(gf_ctx* ctx, int nlev, const double* rho, int precision, int store, gf_stout** out);
+int gf_stout_destroy(gf_stout* st);
+/* calc_smearedU / apply_layer! -> forward! (stout_fast.jl:250-275):
+ * Ubar_mu = exp(TA(C_mu U_mu^dag)) U_mu per level. Uout may be NULL. */
+int gf_stout_forward(gf_ctx* ctx, gf_stout* st, const gf_field* U, gf_field* Uout);
+/* back_prop (Abstractsmearing.jl:316-411) -> layer_pullback! ->
+ * backward_dSdUαUβρ_add! (stout_fast.jl:317-408): dS/dU on the thin links
+ * from dS/dUbar (MAT64/MAT32 in the precision of the stack). */
+int gf_stout_backward(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, gf_field* dSdU);
+/* Smeared Wilson-action MD force on the thin links, the stout-HMC P_update!
+ * (test/HMCstout_test_nowing.jl:99-118): forward, dS/dUbar = beta/2 * staples
+ * of Ubar, back-propagation, P += eps * (-(1/3) TA(U dS/dU)). */
+int gf_stout_mom_update(gf_ctx* ctx, gf_stout* st, gf_field* P, const gf_field* U, double eps, double beta);
+
+/* ---- gradient flow ------------------------------------------------------ */
+/* flow!(U, ::Gradientflow) (smearing/gradientflow.jl:171-238): nsteps RK3
+ * Wilson-flow steps of size eps. */
+int gf_flow(gf_ctx* ctx, gf_field* U, double eps, int nsteps);
+/* add_force!(F, U, temps; plaqonly=true) (AbstractGaugefields.jl:2717-2763):
+ * F += factor * TA(U_mu V_mu^dag) with V the six-staple sum. */
+int gf_flow_force(gf_ctx* ctx, const gf_field* U, gf_field* F, double factor);
+
+/* ---- instrumentation (no counterpart in the reference) ----------------- */
+/* Kernel classes timed by gf_prof_*: */
+#define GF_K_PLAQ 0        /* plaquette / action reduction */
+#define GF_K_FORCE 1       /* staple force (+ momentum update) */
+#define GF_K_LINK_UPDATE 2 /* exp(i eps P) U link update */
+#define GF_K_STOUT_FWD 3   /* stout forward level */
+#define GF_K_BWD_LOCAL 4   /* stout adjoint, local part */
+#define GF_K_BWD_GATHER 5  /* stout adjoint, pull-back gather (+ force) */
+#define GF_K_OTHER 6       /* starts, conversions, kinetic, copies */
+#define GF_K_COUNT 7
+/* Enable (on != 0) or disable CUDA-event timing of every kernel launch on the
+ * context's stream; enabling clears the accumulators. */
+int gf_prof_enable(gf_ctx* ctx, int on);
+/* Total device milliseconds and launch count of one kernel class since the
+ * last gf_prof_enable(ctx, 1); synchronises the context's stream. */
+int gf_prof_read(gf_ctx* ctx, int kernel_class, double* total_ms, long long* launches);
+/* Process-wide number of kernels this library has launched. */
+int gf_launch_count(long long* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GAUGEFIELDS_GB300_H */

@@ -1,0 +1,376 @@
+"""GPU parity: every hot-path entry point of libgfgb300 against the oracle on
+the same seeded inputs, through the C-ABI (via the package's ctypes binding).
+
+Tolerances are those of the target: plaquette and action 1e-13 relative,
+per-link force / links 1e-12 (Frobenius), Delta H 1e-10, stout force 1e-11.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+L4 = (4, 4, 4, 4)
+L8 = (8, 8, 8, 8)
+
+
+def frob_links(A, B):
+    """max over links of the Frobenius norm of the difference."""
+    d = (A - B).reshape(A.shape[0], A.shape[1], -1)
+    return np.sqrt((np.abs(d) ** 2).sum(-1)).max()
+
+
+def frob_mom(A, B):
+    return np.sqrt(((A - B) ** 2).sum(-1)).max()
+
+
+@pytest.fixture(scope="module")
+def hot8(pkg):
+    return pkg.gauge_configuration(L8, start="hot", seed=1234)
+
+
+def test_hot_start_matches_oracle_generator(pkg, oracle):
+    U = pkg.gauge_configuration(L4, start="hot", seed=1234)
+    Uo = oracle.hot_start(list(L4), 1234)
+    assert np.abs(U.to_host() - Uo).max() < 1e-13
+
+
+def test_gaussian_momenta_match_oracle_generator(pkg, oracle):
+    U = pkg.gauge_configuration(L4, start="cold")
+    P = pkg.gaussian_momenta(U, seed=77, sweep=3)
+    assert np.abs(P.to_host() - oracle.gauss_mom(list(L4), 77, 3)).max() < 1e-12
+
+
+def test_upload_download_roundtrip_is_exact(pkg, oracle):
+    U = pkg.gauge_configuration(L4, start="cold")
+    A = oracle.hot_start(list(L4), 5)
+    U.from_host(A)
+    assert np.array_equal(U.to_host(), A)
+    P = pkg.gauge_momenta(U)
+    B = oracle.gauss_mom(list(L4), 9)
+    P.from_host(B)
+    assert np.array_equal(P.to_host(), B)
+
+
+def test_cold_start_invariants(pkg):
+    U = pkg.gauge_configuration(L8, start="cold")
+    assert pkg.measure_plaquette(U) == 1.0
+    P = pkg.gauge_momenta(U)
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, 2.85, "plaquette")
+    drv = pkg.md_driver(U, action, steps=10)
+    res = pkg.md_trajectory_(U, P, drv)
+    assert res.delta_hamiltonian == 0.0
+    assert P * P == 0.0
+    assert pkg.measure_plaquette(U) == pytest.approx(1.0, abs=1e-15)
+
+
+def test_plaquette_and_action(pkg, oracle, hot8):
+    Uh = hot8.to_host()
+    ref = oracle.plaquette(list(L8), Uh)
+    got = pkg.calculate_Plaquette(hot8)
+    assert abs(got - ref) <= 1e-13 * abs(ref)
+    action = pkg.GaugeAction(hot8)
+    pkg.push_(action, 2.85, "plaquette")
+    v = pkg.md_potential(action, hot8)
+    vr = oracle.action(list(L8), Uh, 5.7)
+    assert abs(v - vr) <= 1e-13 * abs(vr)
+
+
+def test_plaquette_is_deterministic(pkg, hot8):
+    a = pkg.calculate_Plaquette(hot8)
+    b = pkg.calculate_Plaquette(hot8)
+    assert a == b
+
+
+def test_construct_staple(pkg, oracle, hot8):
+    Uh = hot8.to_host()
+    V = pkg.Gaugefields4D(hot8.ctx, 4)  # GF_MAT64
+    for mu in (1, 3):
+        pkg.construct_staple_(V, hot8, mu)
+        got = V.to_host()[mu - 1]
+        ref = oracle.staple(list(L8), Uh, mu - 1)
+        assert frob_links(got[None], ref[None]) < 1e-12
+
+
+def test_force(pkg, oracle, hot8):
+    Uh = hot8.to_host()
+    action = pkg.GaugeAction(hot8)
+    pkg.push_(action, 2.85, "plaquette")
+    F = pkg.gauge_momenta(hot8)
+    pkg.md_force_(F, action, hot8)
+    assert frob_mom(F.to_host(), oracle.force(list(L8), Uh, 5.7)) < 1e-12
+
+
+def test_momentum_and_link_updates(pkg, oracle):
+    U = pkg.gauge_configuration(L8, start="hot", seed=11)
+    Uh = U.to_host()
+    P = pkg.gaussian_momenta(U, seed=3)
+    Ph = P.to_host()
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, 2.85, "plaquette")
+    drv = pkg.md_driver(U, action, steps=10, reunitarize=False)
+    pkg.update_momenta_(P, U, 0.1, drv)
+    Ph = Ph + 0.1 * oracle.force(list(L8), Uh, 5.7)
+    assert frob_mom(P.to_host(), Ph) < 1e-12
+    pkg.update_gaugefields_(U, P, 0.05, drv)
+    oracle.link_update(list(L8), Uh, Ph, 0.05)
+    assert frob_links(U.to_host(), Uh) < 1e-12
+
+
+@pytest.mark.parametrize("integrator", ["QPQ", "PQP"])
+def test_trajectory_config1(pkg, oracle, integrator):
+    """8^4 Haar start seed 1234, beta = 5.7, tau = 1, 10 steps, same momenta."""
+    U = pkg.gauge_configuration(L8, start="hot", seed=1234)
+    P = pkg.gaussian_momenta(U, seed=1234, sweep=0)
+    Uh, Ph = U.to_host(), P.to_host()
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, 2.85, "plaquette")
+    integ = pkg.QPQ() if integrator == "QPQ" else pkg.PQP()
+    drv = pkg.md_driver(U, action, steps=10, trajectory_length=1.0, integrator=integ, reunitarize=False)
+    res = pkg.md_trajectory_(U, P, drv)
+    h = oracle.md_trajectory(list(L8), Uh, Ph, 5.7, 1.0, 10, integrator)
+    assert abs(res.initial_hamiltonian - h[0]) <= 1e-13 * abs(h[0])
+    assert abs(res.delta_hamiltonian - h[2]) <= 1e-10
+    assert frob_links(U.to_host(), Uh) < 1e-12
+    assert frob_mom(P.to_host(), Ph) < 1e-12
+
+
+def test_trajectory_with_reunitarisation_stays_within_parity(pkg, oracle):
+    U = pkg.gauge_configuration(L4, start="hot", seed=3)
+    P = pkg.gaussian_momenta(U, seed=4)
+    Uh, Ph = U.to_host(), P.to_host()
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, 2.85, "plaquette")
+    drv = pkg.md_driver(U, action, steps=10, reunitarize=True)
+    res = pkg.md_trajectory_(U, P, drv)
+    h = oracle.md_trajectory(list(L4), Uh, Ph, 5.7, 1.0, 10)
+    assert abs(res.delta_hamiltonian - h[2]) <= 1e-10
+    assert frob_links(U.to_host(), Uh) < 1e-12
+
+
+def test_reversibility_on_gpu(pkg):
+    U = pkg.gauge_configuration(L8, start="hot", seed=1234)
+    P = pkg.gaussian_momenta(U, seed=99)
+    U0, P0 = U.to_host(), P.to_host()
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, 2.85, "plaquette")
+    fwd = pkg.md_driver(U, action, steps=10, trajectory_length=1.0, reunitarize=False)
+    bwd = pkg.md_driver(U, action, steps=10, trajectory_length=-1.0, reunitarize=False)
+    pkg.md_trajectory_(U, P, fwd)
+    pkg.md_trajectory_(U, P, bwd)
+    assert np.abs(U.to_host() - U0).max() < 2e-12
+    assert np.abs(P.to_host() - P0).max() < 2e-12
+
+
+def test_custom_integrator_equals_builtin(pkg):
+    U = pkg.gauge_configuration(L4, start="hot", seed=8)
+    P = pkg.gaussian_momenta(U, seed=8)
+    U2 = U.similar()
+    pkg.substitute_U_(U2, U)
+    P2 = pkg.gauge_momenta(U)
+    P2.from_host(P.to_host())
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, 2.85, "plaquette")
+
+    def my_qpq(U, P, eps, driver):
+        pkg.update_gaugefields_(U, P, eps / 2, driver)
+        pkg.update_momenta_(P, U, eps, driver)
+        pkg.update_gaugefields_(U, P, eps / 2, driver)
+
+    d1 = pkg.md_driver(U, action, steps=5)
+    d2 = pkg.md_driver(U, action, steps=5, integrator=my_qpq)
+    r1 = pkg.md_trajectory_(U, P, d1)
+    r2 = pkg.md_trajectory_(U2, P2, d2)
+    assert abs(r1.delta_hamiltonian - r2.delta_hamiltonian) < 2e-12
+    assert np.abs(U.to_host() - U2.to_host()).max() < 2e-12
+
+
+def test_stout_forward(pkg, oracle):
+    U = pkg.gauge_configuration(L4, start="hot", seed=7)
+    Uh = U.to_host()
+    net = pkg.stout_smearing(U, rho=0.1)
+    pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
+    Ub = pkg.smear(U, net)
+    assert frob_links(Ub.to_host(), oracle.stout_forward(list(L4), Uh, [0.1, 0.1])) < 1e-12
+
+
+def test_stout_backward(pkg, oracle):
+    U = pkg.gauge_configuration(L4, start="hot", seed=7)
+    Uh = U.to_host()
+    rng = np.random.RandomState(5)
+    d = np.ascontiguousarray(rng.randn(4, 256, 3, 3) + 1j * rng.randn(4, 256, 3, 3))
+    net = pkg.stout_smearing(U, rho=0.1)
+    pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
+    res = pkg.smear(U, net, record=True)
+    D = pkg.Gaugefields4D(U.ctx, 4)
+    D.from_host(d)
+    got = pkg.back_prop(D, net, res.history, U).to_host()
+    ref, _ = oracle.stout_backward(list(L4), Uh, [0.1, 0.1], d)
+    assert frob_links(got, ref) < 1e-11
+
+
+@pytest.mark.parametrize("L", [L4, (8, 4, 4, 8)])
+def test_stout_force(pkg, oracle, L):
+    """Smeared-link Wilson force on the thin links, fp64 adjoint vs the oracle."""
+    U = pkg.gauge_configuration(L, start="hot", seed=7)
+    Uh = U.to_host()
+    P = pkg.gauge_momenta(U)
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, 3.0, "plaquette")
+    net = pkg.stout_smearing(U, rho=0.1)
+    pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
+    drv = pkg.md_driver(U, action, steps=1, smearing=net)
+    pkg.update_momenta_(P, U, 1.0, drv)
+    ref = oracle.stout_force(list(L), Uh, [0.1, 0.1], 6.0)
+    assert frob_mom(P.to_host(), ref) < 1e-11
+
+
+def test_stout_force_finite_differences(pkg):
+    """config 3(a): central differences, h = 1e-5, along 16 random su(3)
+    directions at random links of a 4^4 lattice, of the GPU potential."""
+    U = pkg.gauge_configuration(L4, start="hot", seed=7)
+    U0 = U.to_host()
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, 3.0, "plaquette")
+    net = pkg.stout_smearing(U, rho=0.1)
+    pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
+    drv = pkg.md_driver(U, action, steps=1, smearing=net)
+    P = pkg.gauge_momenta(U)
+    pkg.update_momenta_(P, U, 1.0, drv)
+    F = P.to_host()
+    from scipy.linalg import expm
+    from test_oracle import LAM
+    rng = np.random.RandomState(16)
+    h = 1e-5
+    zero = pkg.gauge_momenta(U)
+    worst = 0.0
+    for _ in range(16):
+        mu, x = rng.randint(4), rng.randint(256)
+        w = rng.randn(8)
+        w /= np.linalg.norm(w)
+        G = sum(w[a] * LAM[a] / 2 for a in range(8))
+        vals = []
+        for s in (+1, -1):
+            M = np.swapaxes(U0.copy(), -1, -2)
+            M[mu, x] = expm(1j * s * h * G) @ M[mu, x]
+            U.from_host(np.ascontiguousarray(np.swapaxes(M, -1, -2)))
+            vals.append(pkg.md_hamiltonian(U, zero, drv))
+        fd = (vals[0] - vals[1]) / (2 * h)
+        an = -np.dot(w, F[mu, x])
+        worst = max(worst, abs(fd - an) / max(1.0, abs(an)))
+    assert worst < 1e-6
+
+
+def test_stout_trajectory(pkg, oracle):
+    U = pkg.gauge_configuration(L4, start="hot", seed=7)
+    P = pkg.gaussian_momenta(U, seed=1)
+    Uh, Ph = U.to_host(), P.to_host()
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, 3.0, "plaquette")
+    net = pkg.stout_smearing(U, rho=0.1)
+    pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
+    drv = pkg.md_driver(U, action, steps=5, trajectory_length=0.5, smearing=net, reunitarize=False)
+    res = pkg.md_trajectory_(U, P, drv)
+    h = oracle.md_trajectory(list(L4), Uh, Ph, 6.0, 0.5, 5, rho=[0.1, 0.1])
+    assert abs(res.delta_hamiltonian - h[2]) <= 1e-10
+    assert frob_links(U.to_host(), Uh) < 1e-12
+
+
+def test_mixed_precision_stout_force_is_close(pkg):
+    U = pkg.gauge_configuration(L8, start="hot", seed=7)
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, 3.0, "plaquette")
+    net = pkg.stout_smearing(U, rho=0.1)
+    pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
+    F64 = pkg.gauge_momenta(U)
+    F32 = pkg.gauge_momenta(U)
+    pkg.update_momenta_(F64, U, 1.0, pkg.md_driver(U, action, steps=1, smearing=net))
+    pkg.update_momenta_(F32, U, 1.0, pkg.md_driver(U, action, steps=1, smearing=net, precision="mixed"))
+    a, b = F64.to_host(), F32.to_host()
+    rel = np.abs(a - b).max() / np.abs(a).max()
+    assert rel < 1e-5
+
+
+def test_mixed_precision_trajectory_delta_h(pkg):
+    results = {}
+    for prec in ("fp64", "mixed"):
+        U = pkg.gauge_configuration(L8, start="hot", seed=7)
+        P = pkg.gaussian_momenta(U, seed=1)
+        action = pkg.GaugeAction(U)
+        pkg.push_(action, 3.0, "plaquette")
+        net = pkg.stout_smearing(U, rho=0.1)
+        pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
+        drv = pkg.md_driver(U, action, steps=20, smearing=net, precision=prec)
+        results[prec] = pkg.md_trajectory_(U, P, drv)
+    assert results["mixed"].initial_hamiltonian == results["fp64"].initial_hamiltonian
+    assert abs(results["mixed"].delta_hamiltonian - results["fp64"].delta_hamiltonian) < 1e-4
+
+
+def test_flow(pkg, oracle):
+    U = pkg.gauge_configuration(L4, start="hot", seed=9)
+    Uh = U.to_host()
+    g = pkg.Gradientflow(U, Nflow=10, eps=0.01)
+    pkg.flow_(U, g)
+    oracle.flow(list(L4), Uh, 0.01, 10)
+    assert frob_links(U.to_host(), Uh) < 1e-12
+    assert abs(pkg.calculate_Plaquette(U) - oracle.plaquette(list(L4), Uh)) <= 1e-13 * abs(oracle.plaquette(list(L4), Uh))
+
+
+def test_flow_force(pkg, oracle):
+    U = pkg.gauge_configuration(L4, start="hot", seed=9)
+    F = pkg.gauge_momenta(U)
+    pkg.add_force_(F, U, factor=1.0)
+    assert frob_mom(F.to_host(), oracle.flow_force(list(L4), U.to_host(), 1.0)) < 1e-12
+
+
+def test_flow_golden_value_at_reference_tolerance(pkg, oracle):
+    U = pkg.gauge_configuration(L4, start="cold")
+    U.from_host(oracle.uniform_hot_start(list(L4), 123))
+    pkg.flow_(U, pkg.gradient_flow(U, steps=100, step_size=0.01))
+    assert abs(pkg.measure_plaquette(U) - 0.8786515255315753) / 0.8786515255315753 < 1e-1
+
+
+def test_hmc_update_rejection_restores_links(pkg):
+    U = pkg.gauge_configuration(L4, start="hot", seed=2)
+    P = pkg.gauge_momenta(U)
+    U0 = U.to_host()
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, 2.85, "plaquette")
+    drv = pkg.md_driver(U, action, steps=2, trajectory_length=2.0)  # coarse: large dH
+    res = pkg.hmc_update_(U, P, drv, seed=1, sweep=0, unif=0.999999)
+    if res.accepted:
+        assert res.delta_hamiltonian <= -np.log(0.999999)
+    else:
+        assert np.array_equal(U.to_host(), U0)
+
+
+def test_hmc_physics_smoke(pkg, oracle):
+    """HMC_test_nowing.jl: 4^4 beta = 5.7, tau = 1, 100 steps -> acceptance > 0.5."""
+    U = pkg.gauge_configuration(L4, start="cold")
+    U.from_host(oracle.uniform_hot_start(list(L4), 123))
+    P = pkg.gauge_momenta(U)
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, 2.85, "plaquette")
+    drv = pkg.md_driver(U, action, steps=100)
+    rng = np.random.RandomState(1)
+    acc = sum(pkg.hmc_update_(U, P, drv, seed=77, sweep=t, unif=rng.uniform()).accepted for t in range(10))
+    assert acc / 10 > 0.5
+
+
+def test_errors_are_reported_not_faulted(pkg):
+    U = pkg.gauge_configuration(L4, start="cold")
+    P = pkg.gauge_momenta(U)
+    with pytest.raises(ValueError):
+        pkg.update_gaugefields_(U, P, float("nan"), pkg.md_driver(U, _wilson(pkg, U), steps=1))
+    # kind mismatch: momenta passed as links
+    from gaugefields_gb300 import _lib
+    out = ctypes.c_double()
+    assert _lib.load().gf_plaquette(U.ctx.h, P.field.h, ctypes.byref(out)) == _lib.GF_EINVAL
+
+
+def _wilson(pkg, U):
+    a = pkg.GaugeAction(U)
+    pkg.push_(a, 2.85, "plaquette")
+    return a

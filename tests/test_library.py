@@ -1,0 +1,120 @@
+"""CPU-side checks of the C-ABI library: it builds for sm_103a, loads, exports
+every entry point declared in include/gaugefields_gb300.h, and rejects bad
+arguments with the reference's ArgumentError behaviour before any GPU work."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "gaugefields_gb300.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(gf_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_the_abi():
+    syms = declared_symbols()
+    for s in ("gf_ctx_create", "gf_plaquette", "gf_md_trajectory", "gf_stout_backward", "gf_flow", "gf_last_error"):
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol(pkg):
+    lib = ctypes.CDLL(os.path.join(ROOT, "gaugefields.jl_gb300", "libgfgb300.so"))
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_binding_covers_every_declared_symbol(pkg):
+    from gaugefields_gb300 import _lib
+    assert sorted(declared_symbols()) == sorted(_lib.exported_symbols())
+
+
+def test_library_is_built_for_sm_103a(pkg):
+    from gaugefields_gb300 import _nvcc_build
+    assert "arch=compute_103a,code=sm_103a" in " ".join(_nvcc_build.NVCC_FLAGS)
+    assert _nvcc_build.up_to_date()
+
+
+def test_ctx_create_rejects_bad_extents_before_touching_the_gpu(pkg):
+    from gaugefields_gb300 import _lib
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    for L in ((3, 4, 4, 4), (4, 4, 4, 0), (4, 5, 4, 4)):
+        arr = (ctypes.c_int * 4)(*L)
+        assert lib.gf_ctx_create(arr, 0, ctypes.byref(h)) == _lib.GF_EINVAL
+        assert b"even" in lib.gf_last_error(None)
+    assert lib.gf_ctx_create(None, 0, ctypes.byref(h)) == _lib.GF_EINVAL
+
+
+def test_null_arguments_are_rejected(pkg):
+    from gaugefields_gb300 import _lib
+    lib = _lib.load()
+    out = ctypes.c_double()
+    assert lib.gf_plaquette(None, None, ctypes.byref(out)) == _lib.GF_EINVAL
+    assert lib.gf_md_trajectory(None, None, None, None, None) == _lib.GF_EINVAL
+    assert lib.gf_flow(None, None, ctypes.c_double(0.01), 1) == _lib.GF_EINVAL
+    assert lib.gf_field_free(None) == _lib.GF_OK
+    assert lib.gf_ctx_destroy(None) == _lib.GF_OK
+
+
+def test_python_errors_map_to_argument_errors(pkg):
+    from gaugefields_gb300 import _lib
+    with pytest.raises(ValueError):
+        _lib.call("gf_plaquette", None, None, None)
+
+
+class _FakeU:
+    """Stands in for a configuration in host-side validation tests."""
+
+    def __len__(self):
+        return 4
+
+
+def test_md_driver_argument_validation(pkg):
+    U = _FakeU()
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, 3.0, "plaquette")
+    with pytest.raises(ValueError):
+        pkg.md_driver(U, action, steps=0)
+    with pytest.raises(ValueError):
+        pkg.md_driver(U, action, steps=10, trajectory_length=0.0)
+    with pytest.raises(ValueError):
+        pkg.md_driver(U, action, steps=10, trajectory_length=float("inf"))
+    with pytest.raises(ValueError):
+        pkg.md_driver(U, action, steps=10, integrator=object())
+    with pytest.raises(ValueError):
+        pkg.md_driver(U, pkg.GaugeAction(U), steps=10)  # empty action
+    drv = pkg.md_driver(U, action, steps=10, trajectory_length=-1.0, integrator=pkg.PQP())
+    assert pkg.md_step_size(drv) == -0.1
+    p = drv.params()
+    assert p.beta == 6.0 and p.steps == 10 and p.integrator == 1 and p.nstout == 0
+
+
+def test_md_driver_with_smearing_params(pkg):
+    U = _FakeU()
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, 3.0, "plaquette")
+    net = pkg.stout_smearing(U, rho=0.1)
+    pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.12))
+    drv = pkg.md_driver(U, action, steps=20, smearing=net, precision="mixed")
+    p = drv.params()
+    assert p.nstout == 2 and list(p.rho)[:2] == [0.1, 0.12] and p.precision == 1
+
+
+def test_api_argument_validation(pkg):
+    with pytest.raises(ValueError):
+        pkg.gauge_configuration((4, 4, 4, 4), colors=2)
+    with pytest.raises(ValueError):
+        pkg.gauge_configuration((4, 4, 4, 4), start="warm")
+    with pytest.raises(ValueError):
+        pkg.gauge_configuration((4, 4, 4))
+    with pytest.raises(ValueError):
+        pkg.STOUT_Layer("rectangular", 0.1)
+    with pytest.raises(ValueError):
+        pkg.gradient_flow(None, steps=0)
+    with pytest.raises(ValueError):
+        pkg.gradient_flow(None, step_size=-0.1)
