@@ -9,6 +9,7 @@ Host arrays use the reference's layouts (see include/gaugefields_gb300.h):
             (the column-major (3,3,NX,NY,NZ,NT) array of each direction)
   momenta : float64 array (4, V, 8) indexed [mu, lex, a]
 """
+import atexit
 import ctypes
 import math
 import os
@@ -28,6 +29,20 @@ __all__ = [
     "Gradientflow", "gradient_flow", "flow_", "add_force_", "energy_density_plaquette", "substitute_U_",
     "similar", "clear_U_",
 ]
+
+
+_SHUTDOWN = [False]
+
+
+@atexit.register
+def _mark_shutdown():
+    # At interpreter exit the objects below are finalised in no particular
+    # order; the process is ending, so device memory is left to the driver.
+    _SHUTDOWN[0] = True
+
+
+def _live():
+    return not _SHUTDOWN[0] and _lib._lib is not None
 
 
 class GB300Backend:
@@ -60,7 +75,7 @@ class _Context:
 
     def __del__(self):
         try:
-            if getattr(self, "h", None) and _lib._lib is not None:
+            if getattr(self, "h", None) and _live():
                 _lib._lib.gf_ctx_destroy(self.h)
                 self.h = None
         except Exception:
@@ -87,7 +102,7 @@ class _Field:
 
     def __del__(self):
         try:
-            if getattr(self, "h", None) and _lib._lib is not None:
+            if getattr(self, "h", None) and _live():
                 _lib._lib.gf_field_free(self.h)
                 self.h = None
         except Exception:
@@ -547,7 +562,7 @@ class _StoutStack:
 
     def __del__(self):
         try:
-            if getattr(self, "h", None) and _lib._lib is not None:
+            if getattr(self, "h", None) and _live():
                 _lib._lib.gf_stout_destroy(self.h)
                 self.h = None
         except Exception:

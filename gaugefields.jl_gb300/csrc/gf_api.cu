@@ -196,8 +196,9 @@ extern "C" int gf_field_alloc(gf_ctx* ctx, int kind, gf_field** out) {
 }
 
 extern "C" int gf_field_free(gf_field* f) {
+  // cudaFree waits for outstanding work on the buffer; the context is not
+  // touched, so a field may be freed after its context.
   if (!f) return GF_OK;
-  if (f->ctx) cudaStreamSynchronize(f->ctx->stream);
   field_delete(f);
   return GF_OK;
 }
@@ -375,7 +376,6 @@ extern "C" int gf_stout_create(gf_ctx* ctx, int nlev, const double* rho, int pre
 
 extern "C" int gf_stout_destroy(gf_stout* st) {
   if (!st) return GF_OK;
-  if (st->ctx) cudaStreamSynchronize(st->ctx->stream);
   for (int l = 0; l <= GF_MAX_STOUT; ++l) field_delete(st->lev_in[l]);
   for (int l = 0; l < GF_MAX_STOUT; ++l) field_delete(st->C[l]);
   field_delete(st->Z);
@@ -482,15 +482,22 @@ static void md_run(gf_ctx* ctx, gf_field* U, gf_field* P, const gf_md_params* p,
   }
   double H0 = hamiltonian(ctx, U, P, p);
   double eps = p->tau / p->steps;
-  for (int n = 0; n < p->steps; ++n) {
-    if (p->integrator == GF_QPQ) {
-      link_update(ctx, U, P, 0.5 * eps, p->reunitarize, U32);
+  // Adjacent half steps of consecutive QPQ (PQP) steps act with the same P
+  // (the same U), so they are applied as one full step, as the reference's
+  // _md_fast_qpq! does (molecular_dynamics.jl:618-633): n+1 link updates and
+  // n forces (QPQ), or n+1 forces and n link updates (PQP). The trajectory
+  // is the one of md_step! up to rounding.
+  if (p->integrator == GF_QPQ) {
+    link_update(ctx, U, P, 0.5 * eps, p->reunitarize, U32);
+    for (int n = 0; n < p->steps; ++n) {
       mom_update(ctx, P, U, U32, eps, p);
-      link_update(ctx, U, P, 0.5 * eps, p->reunitarize, U32);
-    } else {
-      mom_update(ctx, P, U, U32, 0.5 * eps, p);
+      link_update(ctx, U, P, (n == p->steps - 1) ? 0.5 * eps : eps, p->reunitarize, U32);
+    }
+  } else {
+    mom_update(ctx, P, U, U32, 0.5 * eps, p);
+    for (int n = 0; n < p->steps; ++n) {
       link_update(ctx, U, P, eps, p->reunitarize, U32);
-      mom_update(ctx, P, U, U32, 0.5 * eps, p);
+      mom_update(ctx, P, U, U32, (n == p->steps - 1) ? 0.5 * eps : eps, p);
     }
   }
   double H1 = hamiltonian(ctx, U, P, p);

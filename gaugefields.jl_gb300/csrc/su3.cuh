@@ -316,24 +316,33 @@ struct ch_coef {
 };
 
 template <typename R>
-GF_HD R ch_eps();
+__device__ __forceinline__ R ch_eps();
 template <>
-GF_HD float ch_eps<float>() { return 3.0e-8f; }
+__device__ __forceinline__ float ch_eps<float>() { return 3.0e-8f; }
 template <>
-GF_HD double ch_eps<double>() { return 5.0e-18; }
+__device__ __forceinline__ double ch_eps<double>() { return 5.0e-18; }
+
+#define GF_CH_TERMS 40
+// 1/n! for n = 0 .. GF_CH_TERMS-1
+static __constant__ double c_inv_fact_d[GF_CH_TERMS] = {1.0, 1.0, 0.5, 0.16666666666666666, 0.041666666666666664, 0.008333333333333333, 0.001388888888888889, 0.0001984126984126984, 2.48015873015873e-05, 2.7557319223985893e-06, 2.755731922398589e-07, 2.505210838544172e-08, 2.08767569878681e-09, 1.6059043836821613e-10, 1.1470745597729725e-11, 7.647163731819816e-13, 4.779477332387385e-14, 2.8114572543455206e-15, 1.5619206968586225e-16, 8.22063524662433e-18, 4.110317623312165e-19, 1.9572941063391263e-20, 8.896791392450574e-22, 3.8681701706306835e-23, 1.6117375710961184e-24, 6.446950284384474e-26, 2.4795962632247972e-27, 9.183689863795546e-29, 3.279889237069838e-30, 1.1309962886447718e-31, 3.7699876288159054e-33, 1.2161250415535181e-34, 3.800390754854744e-36, 1.151633562077195e-37, 3.387157535521162e-39, 9.67759295863189e-41, 2.688220266286636e-42, 7.265460179153071e-44, 1.911963205040282e-45, 4.902469756513544e-47};
+static __constant__ float c_inv_fact_f[GF_CH_TERMS] = {1.0f, 1.0f, 0.5f, 0.166666672f, 0.0416666679f, 0.00833333377f, 0.00138888892f, 0.000198412701f, 2.48015876e-05f, 2.75573188e-06f, 2.755732e-07f, 2.50521079e-08f, 2.08767559e-09f, 1.60590444e-10f, 1.14707454e-11f, 7.64716361e-13f, 4.77947726e-14f, 2.81145736e-15f, 1.56192068e-16f, 8.22063508e-18f, 4.11031759e-19f, 1.95729415e-20f, 8.89679096e-22f, 3.8681703e-23f, 1.61173759e-24f, 6.44695034e-26f, 2.47959628e-27f, 9.18368981e-29f, 3.27988916e-30f, 1.13099625e-31f, 3.76998781e-33f, 1.21612501e-34f, 3.80039067e-36f, 1.1516336e-37f, 3.38715699e-39f, 9.67764745e-41f, 2.68769045e-42f, 7.28675201e-44f, 1.40129846e-45f, 0.0f};
+
+template <typename R>
+__device__ __forceinline__ R inv_fact(int n);
+template <>
+__device__ __forceinline__ double inv_fact<double>(int n) { return c_inv_fact_d[n]; }
+template <>
+__device__ __forceinline__ float inv_fact<float>(int n) { return c_inv_fact_f[n]; }
 
 template <typename R, bool DERIV>
-GF_HD void ch_coefficients(R c0, R c1, ch_coef<R>& out) {
+__device__ __forceinline__ void ch_coefficients(R c0, R c1, ch_coef<R>& out) {
   // power coefficients of Q^n and their partial derivatives
   R a = R(1), b = R(0), c = R(0);
   R a0 = 0, b0 = 0, c0d = 0;  // d/dc0
   R a1 = 0, b1 = 0, c1d = 0;  // d/dc1
-  // running 1/n! and phase i^n (as index n mod 4)
   R fr[3] = {R(1), R(0), R(0)}, fi[3] = {R(0), R(0), R(0)};
   R d1r[3] = {0, 0, 0}, d1i[3] = {0, 0, 0}, d2r[3] = {0, 0, 0}, d2i[3] = {0, 0, 0};
-  R fact = R(1);
-  // bound of |Q^n| coefficient magnitude used for the stopping rule
-  for (int n = 1; n < 64; ++n) {
+  for (int n = 1; n < GF_CH_TERMS; ++n) {
     // advance powers: Q^n from Q^{n-1}
     R na = c0 * c;
     R nb = a + c1 * c;
@@ -347,7 +356,7 @@ GF_HD void ch_coefficients(R c0, R c1, ch_coef<R>& out) {
     a = na; b = nb; c = nc;
     a0 = na0; b0 = nb0; c0d = nc0;
     a1 = na1; b1 = nb1; c1d = nc1;
-    fact = fact / R(n);
+    const R fact = inv_fact<R>(n);
     R ta = a * fact, tb = b * fact, tc = c * fact;
     // i^n: n%4 = 0 -> 1, 1 -> i, 2 -> -1, 3 -> -i
     int ph = n & 3;
@@ -397,7 +406,7 @@ GF_HD void herm_invariants(const mat3<R>& q, R& c0, R& c1) {
 
 // exp(iQ) for traceless Hermitian Q. Q2 receives Q^2 (callers reuse it).
 template <typename R>
-GF_HD mat3<R> expiq(const mat3<R>& q, mat3<R>* q2out = nullptr) {
+__device__ __forceinline__ mat3<R> expiq(const mat3<R>& q, mat3<R>* q2out = nullptr) {
   R c0, c1;
   herm_invariants(q, c0, c1);
   ch_coef<R> cc;
