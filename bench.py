@@ -43,11 +43,11 @@ def workload_name(L):
 # each input field read once, each output written once). fp32 12-real link =
 # 48 B, fp32 3x3 matrix = 72 B, fp64 link = 144 B, fp64 momenta = 64 B.
 # ---------------------------------------------------------------------------
-def algorithmic_bytes_per_link(kclass, precision):
-    if precision == "mixed":
-        link, mat = 48, 72
-    else:
-        link, mat = 144, 144
+def algorithmic_bytes_per_link(kclass):
+    """Compulsory bytes per link of one launch of a kernel class."""
+    fp64 = kclass.endswith("64") or kclass in ("link_update", "plaquette")
+    link, mat = (144, 144) if fp64 else (48, 72)
+    base = kclass[:-2] if kclass.endswith("64") else kclass
     return {
         # U in, Ubar out, C out
         "stout_fwd": link + link + mat,
@@ -55,25 +55,27 @@ def algorithmic_bytes_per_link(kclass, precision):
         "bwd_local": (link + mat + mat + 2 * mat + link + mat + link + 2 * mat) / 2.0,
         # U, Z, Dp in; D out (upper level) or P read+write (bottom level) -- mean
         "bwd_gather": (link + 2 * mat + mat + link + 2 * mat + 128) / 2.0,
-        # P in, U in/out (fp64), fp32 shadow out
-        "link_update": 64 + 144 + 144 + (48 if precision == "mixed" else 0),
+        # P in, U in/out (fp64), fp32 12-real shadow out
+        "link_update": 64 + 144 + 144 + 48,
+        # one link read per link (four directions per site)
         "plaquette": 144,
         "force": link + 128,
-    }.get(kclass)
+    }.get(base)
 
 
 def algorithmic_flops_per_link(kclass):
-    """3x3 complex products counted at 198 flops (216 with accumulation)."""
+    """3x3 complex products counted at 198 flops (216 when accumulated)."""
     mm, mac, rec = 198, 216, 42
     staples = 6 * (mm + mac)  # six staples, two products each
+    base = kclass[:-2] if kclass.endswith("64") else kclass
     return {
-        "stout_fwd": staples + 2 * mm + 600,            # + U S, exp (series + Qh^2), E U
-        "bwd_local": (staples / 2.0) + 8 * mm + 900,      # mean: top level rebuilds staples
+        "stout_fwd": staples + 2 * mm + 600,             # + U S, exp (series + Qh^2), E U
+        "bwd_local": (staples / 2.0) + 8 * mm + 900,     # mean: top level rebuilds staples
         "bwd_gather": 3 * 6 * (mm + mac) + 18 * rec + mm / 2.0,
         "link_update": 2 * mm + 400,
         "plaquette": 2 * mm * 6 / 4.0,
         "force": staples + mm,
-    }.get(kclass)
+    }.get(base)
 
 
 # ---------------------------------------------------------------------------
@@ -161,13 +163,13 @@ def read_peaks():
     return 6800.0, "of fallback (6.8 TB/s)"
 
 
-def read_traffic(kclass, precision, L):
+def read_traffic(kclass, L):
+    """DRAM bytes per launch of a kernel class from the committed ncu summary."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(p):
         return None
     d = json.load(open(p))
-    key = "%s/%s/%d" % (kclass, precision, L)
-    return d.get(key)
+    return d.get("%s/%d" % (kclass, L))
 
 
 # ---------------------------------------------------------------------------
@@ -246,17 +248,20 @@ def e2e_hmc(pkg, torch, L, steps, warmup, rank):
     hR = torch.empty((4, V, 3, 3), dtype=torch.complex128, pin_memory=True).numpy()
     hU[...] = U.to_host()
     rng = np.random.RandomState(77 + rank)
+    # each step's momenta, generated beforehand into pinned host buffers
     moms = []
     for k in range(2):
         pkg.gaussian_momenta_(P, seed=SEED, sweep=1000 + k)
-        moms.append(P.to_host())
+        buf = hP if k == 0 else torch.empty((4, V, 8), dtype=torch.float64, pin_memory=True).numpy()
+        buf[...] = P.to_host()
+        moms.append(buf)
     prm = drv.params()
     out = (ctypes.c_double * 3)()
 
     def step(k):
-        hP[...] = moms[k % 2]
+        hm = moms[k % 2]
         _lib.check(lib.gf_upload_links(U.ctx.h, U.field.h, ctypes.c_void_p(hU.ctypes.data)), U.ctx.h)
-        _lib.check(lib.gf_upload_mom(U.ctx.h, P.field.h, ctypes.c_void_p(hP.ctypes.data)), U.ctx.h)
+        _lib.check(lib.gf_upload_mom(U.ctx.h, P.field.h, ctypes.c_void_p(hm.ctypes.data)), U.ctx.h)
         _lib.check(lib.gf_md_trajectory(U.ctx.h, U.field.h, P.field.h, ctypes.byref(prm), out), U.ctx.h)
         if rng.uniform() < np.exp(-out[2]):
             _lib.check(lib.gf_download_links(U.ctx.h, U.field.h, ctypes.c_void_p(hU.ctypes.data)), U.ctx.h)
@@ -277,15 +282,26 @@ def e2e_hmc(pkg, torch, L, steps, warmup, rank):
             "d2h_bytes_per_step": 36 * V * 16 + 3 * 8, "ms_per_step": 1e3 * sec / steps}
 
 
-def dh_check(pkg, L):
-    """Delta H of one trajectory from the same start and momenta in both forms."""
+def dh_check(pkg, L, ntherm):
+    """|Delta H_mixed - Delta H_fp64| for one trajectory from the same
+    configuration and momenta. The configuration is thermalised first: cold
+    start, then `ntherm` mixed-precision trajectories kept unconditionally."""
+    U, P, drv = make_setup(pkg, L, "mixed", SEED)
+    pkg._lib.call("gf_cold_start", U.ctx.h, U.field.h, ctx=U.ctx.h)
+    for t in range(ntherm):
+        pkg.gaussian_momenta_(P, seed=SEED + 5, sweep=t)
+        pkg.md_trajectory_(U, P, drv)
+    Ut = U.to_host()
+    plaq = pkg.measure_plaquette(U)
     res = {}
     for prec in ("fp64", "mixed"):
-        U, P, drv = make_setup(pkg, L, prec, SEED)
-        pkg.gaussian_momenta_(P, seed=SEED, sweep=0)
-        res[prec] = pkg.md_trajectory_(U, P, drv).delta_hamiltonian
+        U2, P2, drv2 = make_setup(pkg, L, prec, SEED)
+        U2.from_host(Ut)
+        pkg.gaussian_momenta_(P2, seed=SEED, sweep=10 ** 6)
+        res[prec] = pkg.md_trajectory_(U2, P2, drv2).delta_hamiltonian
+        del U2, P2, drv2
     return {"dH_fp64": res["fp64"], "dH_mixed": res["mixed"], "abs_diff": abs(res["mixed"] - res["fp64"]),
-            "start": "Haar seed 7 (unthermalised), momenta seed 7"}
+            "start": "cold start + %d mixed trajectories kept unconditionally (plaquette %.6f)" % (ntherm, plaq)}
 
 
 def oracle_sample(threads, L_sample=16, md_steps=None):
@@ -367,6 +383,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--therm", type=int, default=10, help="thermalisation trajectories before the Delta H check")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -405,7 +422,7 @@ def main():
         s64, _, _, _, _ = timed_hmc(pkg, torch, U, P, drv, 1, 1, rank, None)
         fp64 = {"value": 1.0 / s64, "unit": UNIT, "ms_per_step": 1e3 * s64, "steps": 1, "warmup": 1}
         del U, P, drv
-    dh = dh_check(pkg, L) if not args.no_fp64 else None
+    dh = dh_check(pkg, L, args.therm) if not args.no_fp64 else None
 
     e2e = None
     if not args.no_e2e:
@@ -414,23 +431,26 @@ def main():
     # roofline of the dominant kernel (device time from CUDA events in the timed region)
     roof, compute = None, None
     if kern:
+        from gaugefields_gb300 import _lib as glib
         dom = max(kern, key=lambda k: kern[k]["ms"])
         d = kern[dom]
         per_launch_s = d["ms"] / d["launches"] / 1e3
-        bpl = algorithmic_bytes_per_link(dom, "mixed")
-        alg_bytes = bpl * 4 * V
+        alg_bytes = algorithmic_bytes_per_link(dom) * 4 * V
         achieved = alg_bytes / per_launch_s / 1e9
+        prec = glib.KERNEL_PRECISION[dom]
         roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "peak_note": hbm_note, "algorithmic_bytes_per_launch": alg_bytes,
-                "traffic": read_traffic(dom, "mixed", L), "launches": d["launches"],
-                "avg_launch_ms": 1e3 * per_launch_s}
+                "traffic": read_traffic(dom, L), "launches": d["launches"], "avg_launch_ms": 1e3 * per_launch_s}
         fl = algorithmic_flops_per_link(dom) * 4 * V
-        compute = {"kernel": dom, "achieved_tflops": fl / per_launch_s / 1e12, "peak_tflops": peaks["fp32_tflops"],
-                   "peak_note": "cuBLAS sgemm (no TF32) measured in this run", "flops_per_launch": fl,
-                   "frac": fl / per_launch_s / 1e12 / peaks["fp32_tflops"]}
+        pk = peaks["fp64_tflops"] if prec == "fp64" else peaks["fp32_tflops"]
+        compute = {"kernel": dom, "precision": prec, "achieved_tflops": fl / per_launch_s / 1e12, "peak_tflops": pk,
+                   "peak_note": "cuBLAS %s measured in this run" % ("dgemm" if prec == "fp64" else "sgemm (no TF32)"),
+                   "flops_per_launch": fl, "frac": fl / per_launch_s / 1e12 / pk,
+                   "binding": "fp64 issue" if prec == "fp64" else "fp32 issue / L1"}
         total_ms = sum(v["ms"] for v in kern.values())
         for k in kern:
             kern[k]["share"] = kern[k]["ms"] / total_ms
+            kern[k]["avg_ms"] = kern[k]["ms"] / kern[k]["launches"]
 
     cpu = None
     if not args.no_cpu and rank == 0:

@@ -97,8 +97,12 @@ SIGNATURES = {
     "gf_launch_count": [ctypes.POINTER(ctypes.c_longlong)],
 }
 
-GF_K_PLAQ, GF_K_FORCE, GF_K_LINK_UPDATE, GF_K_STOUT_FWD, GF_K_BWD_LOCAL, GF_K_BWD_GATHER, GF_K_OTHER = range(7)
-KERNEL_CLASSES = ["plaquette", "force", "link_update", "stout_fwd", "bwd_local", "bwd_gather", "other"]
+KERNEL_CLASSES = ["plaquette", "force", "link_update", "stout_fwd", "bwd_local", "bwd_gather", "stout_fwd64",
+                  "bwd_local64", "bwd_gather64", "other"]
+# arithmetic precision of each class (the force class follows its links)
+KERNEL_PRECISION = {"plaquette": "fp64", "force": "fp32", "link_update": "fp64", "stout_fwd": "fp32",
+                    "bwd_local": "fp32", "bwd_gather": "fp32", "stout_fwd64": "fp64", "bwd_local64": "fp64",
+                    "bwd_gather64": "fp64", "other": "fp64"}
 
 _lib = None
 

@@ -242,7 +242,7 @@ template <typename R>
 static void forward_impl(gf_ctx* ctx, gf_stout* st) {
   dim3 grid(blocks_for(ctx->geom.vol, 128), 4);
   for (int l = 0; l < st->nlev; ++l) {
-    ProfScope prof(ctx, GF_K_STOUT_FWD);
+    ProfScope prof(ctx, sizeof(R) == 8 ? GF_K_STOUT_FWD64 : GF_K_STOUT_FWD);
     k_stout_fwd<R><<<grid, 128, 0, ctx->stream>>>(
         src_of<R>(st->lev_in[l]), (typename Prec<R>::LinkElem*)st->lev_in[l + 1]->ptr,
         st->store ? (typename Prec<R>::MatElem*)st->C[l]->ptr : nullptr, ctx->geom, (R)st->rho[l]);
@@ -289,7 +289,7 @@ static void backward_impl(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, do
     const ME* Cst = st->store ? (const ME*)st->C[l]->ptr : nullptr;
     const ME* din = (l == st->nlev - 1) ? dbar : (const ME*)st->D[cur]->ptr;
     {
-    ProfScope prof(ctx, GF_K_BWD_LOCAL);
+    ProfScope prof(ctx, sizeof(R) == 8 ? GF_K_BWD_LOCAL64 : GF_K_BWD_LOCAL);
     if (top) {
       k_bwd_local<R, true><<<grid, 128, 0, ctx->stream>>>(src_of<R>(st->lev_in[l]), src_of<R>(st->lev_in[l + 1]),
                                                           nullptr, Cst, (ME*)st->Z->ptr, (ME*)st->Dp->ptr, ctx->geom,
@@ -302,7 +302,7 @@ static void backward_impl(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, do
     GF_CHECK_LAUNCH();
     }
     int nxt = cur ^ 1;
-    ProfScope prof(ctx, GF_K_BWD_GATHER);
+    ProfScope prof(ctx, sizeof(R) == 8 ? GF_K_BWD_GATHER64 : GF_K_BWD_GATHER);
     if (l == 0 && P) {
       k_bwd_gather<R, true><<<grid, 128, 0, ctx->stream>>>(src_of<R>(st->lev_in[0]), (const ME*)st->Z->ptr,
                                                            (const ME*)st->Dp->ptr, nullptr, (double*)P->ptr,

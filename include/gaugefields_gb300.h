@@ -188,14 +188,17 @@ int gf_flow_force(gf_ctx* ctx, const gf_field* U, gf_field* F, double factor);
 
 /* ---- instrumentation (no counterpart in the reference) ----------------- */
 /* Kernel classes timed by gf_prof_*: */
-#define GF_K_PLAQ 0        /* plaquette / action reduction */
-#define GF_K_FORCE 1       /* staple force (+ momentum update) */
-#define GF_K_LINK_UPDATE 2 /* exp(i eps P) U link update */
-#define GF_K_STOUT_FWD 3   /* stout forward level */
-#define GF_K_BWD_LOCAL 4   /* stout adjoint, local part */
-#define GF_K_BWD_GATHER 5  /* stout adjoint, pull-back gather (+ force) */
-#define GF_K_OTHER 6       /* starts, conversions, kinetic, copies */
-#define GF_K_COUNT 7
+#define GF_K_PLAQ 0         /* plaquette / action reduction (fp64) */
+#define GF_K_FORCE 1        /* Wilson staple force (+ momentum update) */
+#define GF_K_LINK_UPDATE 2  /* exp(i eps P) U link update (fp64) */
+#define GF_K_STOUT_FWD 3    /* stout forward level, fp32 */
+#define GF_K_BWD_LOCAL 4    /* stout adjoint, local part, fp32 */
+#define GF_K_BWD_GATHER 5   /* stout adjoint, pull-back gather (+ force), fp32 */
+#define GF_K_STOUT_FWD64 6  /* the same three stages in fp64 */
+#define GF_K_BWD_LOCAL64 7
+#define GF_K_BWD_GATHER64 8
+#define GF_K_OTHER 9        /* starts, conversions, kinetic, copies */
+#define GF_K_COUNT 10
 /* Enable (on != 0) or disable CUDA-event timing of every kernel launch on the
  * context's stream; enabling clears the accumulators. */
 int gf_prof_enable(gf_ctx* ctx, int on);

@@ -106,6 +106,19 @@ static inline void stm(cdbl* U, const Lat* l, int mu, long lex, const M3* a) {
     for (int j = 0; j < 3; ++j) p[i + 3 * j] = a->m[i][j];
 }
 
+/* Neumaier (improved Kahan) summation of n doubles: the oracle's global sums
+ * are accurate to a few ulp of the total, independent of their order. */
+static double sum_accurate(const double* v, long n) {
+  double s = 0.0, c = 0.0;
+  for (long i = 0; i < n; ++i) {
+    double t = s + v[i];
+    if (fabs(s) >= fabs(v[i])) c += (s - t) + v[i];
+    else c += (v[i] - t) + s;
+    s = t;
+  }
+  return s + c;
+}
+
 static inline M3 mzero(void) {
   M3 a;
   memset(&a, 0, sizeof a);
@@ -198,7 +211,57 @@ static M3 exp_t4(double v1, double v3, double v4, double v5, double v6, double v
   return E;
 }
 
+/* Which exponential the oracle's link updates use: 0 = the reference's eigen
+ * method (default), 1 = Taylor series with scaling and squaring to full
+ * double precision (used to separate the eigen method's own ~1e-14 error
+ * from differences of the GPU path). */
+static int g_exp_method = 0;
+void or_set_exp_method(int m) { g_exp_method = m; }
+
+static M3 expt_taylor(double t, const double* u) {
+  /* X = i t sum_a u_a lambda_a / 2, exp(X) = (exp(X / 2^k))^(2^k) */
+  M3 X;
+  double c[8];
+  for (int a = 0; a < 8; ++a) c[a] = t * u[a] * 0.5;
+  X.m[0][0] = I * (c[2] + sr3i * c[7]);
+  X.m[1][1] = I * (-c[2] + sr3i * c[7]);
+  X.m[2][2] = I * (-2 * sr3i * c[7]);
+  X.m[0][1] = I * (c[0] - I * c[1]);
+  X.m[1][0] = I * (c[0] + I * c[1]);
+  X.m[0][2] = I * (c[3] - I * c[4]);
+  X.m[2][0] = I * (c[3] + I * c[4]);
+  X.m[1][2] = I * (c[5] - I * c[6]);
+  X.m[2][1] = I * (c[5] + I * c[6]);
+  double nrm = 0;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) nrm += creal(X.m[i][j] * conj(X.m[i][j]));
+  nrm = sqrt(nrm);
+  int k = 0;
+  while (nrm > 0.25) {
+    nrm *= 0.5;
+    ++k;
+  }
+  double sc = ldexp(1.0, -k);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) X.m[i][j] *= sc;
+  M3 E = meye(), term = meye();
+  for (int n = 1; n <= 24; ++n) {
+    term = mmul(&term, &X);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) term.m[i][j] /= n;
+    madd(&E, 1.0, &term);
+  }
+  for (int r = 0; r < k; ++r) E = mmul(&E, &E);
+  return E;
+}
+
+static M3 expt_eigen_ref(double t, const double* u);
+
 static M3 expt_eigen(double t, const double* u) {
+  return g_exp_method == 1 ? expt_taylor(t, u) : expt_eigen_ref(t, u);
+}
+
+static M3 expt_eigen_ref(double t, const double* u) {
   const double pi23 = 2.0 * M_PI / 3.0;
   const double tinyvalue = 1e-100;
   double c1 = t * u[0] * 0.5, c2 = t * u[1] * 0.5, c3 = t * u[2] * 0.5, c4 = t * u[3] * 0.5;
@@ -524,8 +587,7 @@ double or_plaquette(const int L[4], const cdbl* U) {
     }
     part[x] = creal(s * 0.5);
   }
-  double sum = 0;
-  for (long x = 0; x < lat.V; ++x) sum += part[x];
+  double sum = sum_accurate(part, lat.V);
   free(part);
   return sum;
 }
@@ -569,8 +631,7 @@ double or_action(const int L[4], const cdbl* U, double beta) {
       }
     part[x] = creal(s);
   }
-  double sum = 0;
-  for (long x = 0; x < lat.V; ++x) sum += part[x];
+  double sum = sum_accurate(part, lat.V);
   free(part);
   return -sum / 3.0;
 }
@@ -635,9 +696,11 @@ static void exp_af_u(const Lat* lat, cdbl* W, double a, const double* F, const c
 
 double or_kinetic(const int L[4], const double* P) {
   Lat lat = mklat(L);
-  double s = 0;
   size_t n = (size_t)32 * lat.V;
-  for (size_t i = 0; i < n; ++i) s += P[i] * P[i];
+  double* sq = (double*)malloc(sizeof(double) * n);
+  for (size_t i = 0; i < n; ++i) sq[i] = P[i] * P[i];
+  double s = sum_accurate(sq, (long)n);
+  free(sq);
   return s;
 }
 

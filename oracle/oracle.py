@@ -54,6 +54,7 @@ def _declare(l):
         "or_num_threads": ([], _I),
         "or_set_threads": ([_I], None),
         "or_taylor_fallbacks": ([], ctypes.c_long),
+        "or_set_exp_method": ([_I], None),
         "or_staple": ([_P, _P, _I, _P], None),
         "or_plaquette": ([_P, _P], _D),
         "or_dsdu": ([_P, _P, _D, _I, _P], None),
@@ -125,6 +126,12 @@ def set_threads(n):
 
 def num_threads():
     return lib().or_num_threads()
+
+
+def set_exp_method(name):
+    """'eigen' (the reference's exptU!, default) or 'taylor' (full double
+    precision); the choice applies to link updates, flow steps and stout."""
+    lib().or_set_exp_method({"eigen": 0, "taylor": 1}[name])
 
 
 def taylor_fallbacks():
