@@ -95,6 +95,7 @@ SIGNATURES = {
     "gf_prof_enable": [_P, _I],
     "gf_prof_read": [_P, _I, _DP, ctypes.POINTER(ctypes.c_longlong)],
     "gf_launch_count": [ctypes.POINTER(ctypes.c_longlong)],
+    "gf_plaquette_noalloc": [_P, ctypes.POINTER(ctypes.c_int), _P, _P],
 }
 
 KERNEL_CLASSES = ["plaquette", "force", "link_update", "stout_fwd", "bwd_local", "bwd_gather", "stout_fwd64",

@@ -15,6 +15,7 @@ static std::atomic<long long> g_launches(0);
 
 namespace gf {
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void set_global_error(const std::string& m) { g_last_error = m; }
 
 void prof_begin(gf_ctx* ctx, int kid) {
   if (!ctx->prof_on) return;

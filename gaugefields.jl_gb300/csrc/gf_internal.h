@@ -103,6 +103,9 @@ struct ProfScope {
   ~ProfScope() { prof_end(c, k); }
 };
 
+// message returned by gf_last_error(NULL) for calls without a context
+void set_global_error(const std::string& m);
+
 // ---- reductions (gf_fields.cu) ----
 // Deterministic two-stage sum of per-site doubles produced by a kernel that
 // writes one partial per block; returns the total on the host.

@@ -186,6 +186,25 @@ int gf_flow(gf_ctx* ctx, gf_field* U, double eps, int nsteps);
  * F += factor * TA(U_mu V_mu^dag) with V the six-staple sum. */
 int gf_flow_force(gf_ctx* ctx, const gf_field* U, gf_field* F, double factor);
 
+/* ---- allocation-free plaquette (no counterpart in the reference) -------- */
+/* The plaquette sum of gf_plaquette for callers that cannot allocate device
+ * memory: applications whose device memory belongs to another allocator
+ * (CUDA.jl's pool, PyTorch's caching allocator) and loops where a cudaMalloc
+ * would synchronise the device. It needs no context (creating one
+ * allocates). `links` is the device storage of a GF_LINK64 field
+ * (gf_field_device_ptr) for the lattice L = {NX,NY,NZ,NT}; `out` is one
+ * double in device memory; `stream` a cudaStream_t (NULL: default stream).
+ * Kernels are only enqueued: read `out` after the stream has finished.
+ * The per-block partial sums live in a fixed 1 MiB device array inside the
+ * library (held by every GPU that loads it until the process exits), so the
+ * lattice may have at most 16,777,216 sites (64^4); larger lattices return
+ * GF_EINVAL. All calls share that array: calls whose kernels overlap on the
+ * GPU race and must be serialised by the caller. The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current; make it before any stream capture. gf_last_error(NULL) gives the
+ * message of a failed call. */
+int gf_plaquette_noalloc(const void* links, const int L[4], double* out, void* stream);
+
 /* ---- instrumentation (no counterpart in the reference) ----------------- */
 /* Kernel classes timed by gf_prof_*: */
 #define GF_K_PLAQ 0         /* plaquette / action reduction (fp64) */
