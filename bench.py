@@ -373,6 +373,29 @@ def run_reference(args):
     return 0
 
 
+def run_kernel_mode(args):
+    """Small single-family cases for profiler captures: `force` repeats the
+    mixed stout force (gf_stout_mom_update), `link` the fp64 link update."""
+    import torch
+    import __graft_entry__ as entry
+    pkg = entry.build()
+    L = args.lattice
+    U, P, drv = make_setup(pkg, L, "mixed", SEED)
+    pkg.gaussian_momenta_(P, seed=SEED)
+    calls = []
+    for k in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if args.mode == "force":
+            pkg.update_momenta_(P, U, 0.01, drv)
+        else:
+            pkg.update_gaugefields_(U, P, 0.01, drv)
+        U.ctx.sync()
+        calls.append(time.perf_counter() - t0)
+    print(json.dumps({"mode": args.mode, "lattice": [L] * 4, "ms_per_call": 1e3 * min(calls[args.warmup:])}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -384,9 +407,13 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--therm", type=int, default=10, help="thermalisation trajectories before the Delta H check")
+    ap.add_argument("--mode", default="hmc", choices=["hmc", "force", "link"],
+                    help="hmc: the benchmark; force/link: one kernel family, for profiler captures")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode != "hmc":
+        return run_kernel_mode(args)
 
     import torch
     rank = int(os.environ.get("RANK", "0"))

@@ -109,6 +109,8 @@ extern "C" int gf_ctx_create(const int L[4], int device, gf_ctx** out) {
   GF_CUDA(cudaMalloc(&ctx->d_partials, sizeof(double) * ctx->partial_cap));
   GF_CUDA(cudaMalloc(&ctx->d_result, sizeof(double) * 4));
   GF_CUDA(cudaMallocHost(&ctx->h_result, sizeof(double) * 4));
+  GF_CUDA(cudaMalloc(&ctx->d_hash, sizeof(unsigned long long)));
+  GF_CUDA(cudaMallocHost(&ctx->h_hash, sizeof(unsigned long long)));
   *out = ctx;
   return GF_OK;
   }
@@ -139,6 +141,8 @@ extern "C" int gf_ctx_destroy(gf_ctx* ctx) {
   if (ctx->d_partials) cudaFree(ctx->d_partials);
   if (ctx->d_result) cudaFree(ctx->d_result);
   if (ctx->h_result) cudaFreeHost(ctx->h_result);
+  if (ctx->d_hash) cudaFree(ctx->d_hash);
+  if (ctx->h_hash) cudaFreeHost(ctx->h_hash);
   if (ctx->prof_ev) {
     for (int i = 0; i < 2 * GF_PROF_CAP; ++i) cudaEventDestroy(ctx->prof_ev[i]);
     delete[] ctx->prof_ev;
@@ -472,7 +476,33 @@ static void mom_update(gf_ctx* ctx, gf_field* P, const gf_field* U, const gf_fie
   stout_backward(ctx, st, nullptr, p->beta, nullptr, P, eps);
 }
 
-static void md_run(gf_ctx* ctx, gf_field* U, gf_field* P, const gf_md_params* p, double out[3]) {
+// The potential at the start of a trajectory is the one the previous MD call
+// ended on (accepted) or started from (rejected, links restored). It is reused
+// when a 64-bit hash of the fp64 links and the action parameters match, which
+// saves one fp64 stout forward + plaquette per trajectory; any change of the
+// links changes the hash, so a reused value is bitwise the recomputed one.
+static bool vcache_hit(const gf_ctx* ctx, const gf_md_params* p, unsigned long long h) {
+  if (!ctx->vc_valid || ctx->vc_hash != h || ctx->vc_beta != p->beta || ctx->vc_nstout != p->nstout) return false;
+  for (int l = 0; l < p->nstout; ++l)
+    if (ctx->vc_rho[l] != p->rho[l]) return false;
+  return true;
+}
+
+static void vcache_set(gf_ctx* ctx, const gf_md_params* p, unsigned long long h, double V) {
+  ctx->vc_valid = 1;
+  ctx->vc_hash = h;
+  ctx->vc_V = V;
+  ctx->vc_beta = p->beta;
+  ctx->vc_nstout = p->nstout;
+  for (int l = 0; l < GF_MAX_STOUT; ++l) ctx->vc_rho[l] = l < p->nstout ? p->rho[l] : 0.0;
+}
+
+struct MDResult {
+  double H0, H1, V0, V1;
+  unsigned long long h0, h1;
+};
+
+static MDResult md_run(gf_ctx* ctx, gf_field* U, gf_field* P, const gf_md_params* p) {
   need_kind(U, GF_LINK64, "md: U");
   need_kind(P, GF_MOM64, "md: P");
   gf_field* U32 = nullptr;
@@ -481,7 +511,10 @@ static void md_run(gf_ctx* ctx, gf_field* U, gf_field* P, const gf_md_params* p,
     U32 = ctx->w_link32;
     link64_to_32(ctx, U32, U);
   }
-  double H0 = hamiltonian(ctx, U, P, p);
+  MDResult r;
+  r.h0 = field_hash(ctx, U);
+  r.V0 = vcache_hit(ctx, p, r.h0) ? ctx->vc_V : potential(ctx, U, p);
+  r.H0 = r.V0 + 0.5 * kinetic(ctx, P);
   double eps = p->tau / p->steps;
   // Adjacent half steps of consecutive QPQ (PQP) steps act with the same P
   // (the same U), so they are applied as one full step, as the reference's
@@ -501,10 +534,10 @@ static void md_run(gf_ctx* ctx, gf_field* U, gf_field* P, const gf_md_params* p,
       mom_update(ctx, P, U, U32, (n == p->steps - 1) ? 0.5 * eps : eps, p);
     }
   }
-  double H1 = hamiltonian(ctx, U, P, p);
-  out[0] = H0;
-  out[1] = H1;
-  out[2] = H1 - H0;
+  r.V1 = potential(ctx, U, p);
+  r.H1 = r.V1 + 0.5 * kinetic(ctx, P);
+  r.h1 = field_hash(ctx, U);
+  return r;
 }
 
 extern "C" int gf_force(gf_ctx* ctx, const gf_field* U, double beta, gf_field* F) {
@@ -557,8 +590,15 @@ extern "C" int gf_md_trajectory(gf_ctx* ctx, gf_field* U, gf_field* P, const gf_
   need_ctx(ctx, U);
   need_ctx(ctx, P);
   check_md(prm);
-  md_run(ctx, U, P, prm, out);
-  if (!std::isfinite(out[2])) throw gf_error(GF_ENAN, "gf_md_trajectory: Delta H is not finite");
+  MDResult r = md_run(ctx, U, P, prm);
+  out[0] = r.H0;
+  out[1] = r.H1;
+  out[2] = r.H1 - r.H0;
+  if (!std::isfinite(out[2])) {
+    ctx->vc_valid = 0;
+    throw gf_error(GF_ENAN, "gf_md_trajectory: Delta H is not finite");
+  }
+  vcache_set(ctx, prm, r.h1, r.V1);
   API_END(ctx)
 }
 
@@ -574,12 +614,15 @@ extern "C" int gf_hmc_update(gf_ctx* ctx, gf_field* U, gf_field* P, const gf_md_
   if (!ctx->w_link64) ctx->w_link64 = field_new(ctx, GF_LINK64);
   copy_field(ctx, ctx->w_link64, U);
   gaussian_momenta(ctx, P, seed, sweep);
-  double h[3];
-  md_run(ctx, U, P, prm, h);
+  MDResult r = md_run(ctx, U, P, prm);
+  double h[3] = {r.H0, r.H1, r.H1 - r.H0};
   bool finite = std::isfinite(h[2]);
   bool accept = finite && (h[2] <= 0.0 || unif < std::exp(-h[2]));
   if (!accept) copy_field(ctx, U, ctx->w_link64);
   GF_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (accept) vcache_set(ctx, prm, r.h1, r.V1);
+  else if (std::isfinite(r.V0)) vcache_set(ctx, prm, r.h0, r.V0);
+  else ctx->vc_valid = 0;
   out[0] = h[0];
   out[1] = h[1];
   out[2] = h[2];

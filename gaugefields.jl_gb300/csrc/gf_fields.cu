@@ -106,6 +106,31 @@ double kinetic(gf_ctx* ctx, const gf_field* P) {
   return finish_reduction(ctx, nb);
 }
 
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  // splitmix64 finaliser (Steele, Lea, Flood, "Fast splittable pseudorandom
+  // number generators", OOPSLA 2014)
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__global__ void k_hash(const unsigned long long* __restrict__ w, size_t n, unsigned long long* __restrict__ out) {
+  unsigned long long h = 0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    h += mix64(w[i] ^ (i * 0x9E3779B97F4A7C15ull));
+  for (int o = 16; o > 0; o >>= 1) h += __shfl_down_sync(0xffffffffu, h, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, h);
+}
+
+unsigned long long field_hash(gf_ctx* ctx, const gf_field* f) {
+  GF_CUDA(cudaMemsetAsync(ctx->d_hash, 0, sizeof(unsigned long long), ctx->stream));
+  k_hash<<<152 * 8, 256, 0, ctx->stream>>>((const unsigned long long*)f->ptr, f->bytes / 8, ctx->d_hash);
+  GF_CHECK_LAUNCH();
+  GF_CUDA(cudaMemcpyAsync(ctx->h_hash, ctx->d_hash, sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+  GF_CUDA(cudaStreamSynchronize(ctx->stream));
+  return *ctx->h_hash;
+}
+
 // ---------------------------------------------------------------------------
 // reference layout <-> device layout
 // host links: complex (i,j,x,y,z,t) column-major, element (i,j) of direction

@@ -61,6 +61,15 @@ struct gf_ctx {
   gf_stout* w_stout32;    // stout workspace, fp32
   int w_stout_nlev;
   double w_stout_rho[GF_MAX_STOUT];
+  // potential of the last configuration an MD call ended on, keyed by a
+  // 64-bit hash of its fp64 links and the action parameters
+  unsigned long long* d_hash;
+  unsigned long long* h_hash;
+  int vc_valid;
+  unsigned long long vc_hash;
+  double vc_V, vc_beta;
+  int vc_nstout;
+  double vc_rho[GF_MAX_STOUT];
   // per-kernel CUDA-event timing on the context's stream (gf_prof_*)
   int prof_on;
   int prof_n;
@@ -111,6 +120,8 @@ void set_global_error(const std::string& m);
 // writes one partial per block; returns the total on the host.
 double finish_reduction(gf_ctx* ctx, int nblocks);
 double kinetic(gf_ctx* ctx, const gf_field* P);
+// order-independent 64-bit hash of a field's bytes (sum of mixed words)
+unsigned long long field_hash(gf_ctx* ctx, const gf_field* f);
 
 // ---- field plumbing (gf_fields.cu) ----
 void upload_links(gf_ctx* ctx, gf_field* U, const double* host);

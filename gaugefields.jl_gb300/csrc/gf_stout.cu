@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(128)
   herm_invariants(qh, c0, c1);
   ch_coef<R> cc;
   ch_coefficients<R, true>(c0, c1, cc);
-  mat3<R> qh2 = mul_nn(qh, qh);
+  mat3<R> qh2 = herm_square(qh);
   mat3<R> db;
   if (TOP) db = scale(halfbeta, staple_sum<R>(mu, Utop, g, st, s));
   else db = LinkFull<R>::load(Dbar, mu, s, V);
@@ -163,24 +163,26 @@ __device__ __forceinline__ void gather_axis(mat3<R>& acc, const typename Prec<R>
   {
     mat3<R> a1 = U(K, xpn, V);   // U_K(x+nu)
     mat3<R> a2 = U(NU, xpk, V);  // U_nu(x+K)
-    mat3<R> t = mul_na(a1, a2);
-    mac_nn(acc, t, LinkFull<R>::load(Z, K, s, V));  // (a)
-    mat3<R> a6 = U(K, s, V);  // U_K(x)
-    t = mul_nn(a1, LinkFull<R>::load(Z, NU, xpk, V));
-    mac_na(acc, t, a6);  // (f)
+    mat3<R> a6 = U(K, s, V);     // U_K(x)
+    // (a) + (f) = U_K(x+nu) [U_nu(x+K)^dag Z_K(x) + Z_nu(x+K) U_K(x)^dag]
+    mat3<R> t = mul_an(a2, LinkFull<R>::load(Z, K, s, V));
+    mac_na(t, LinkFull<R>::load(Z, NU, xpk, V), a6);
+    mac_nn(acc, a1, t);
+    // (c) = Z_K(x+nu)^dag [U_K(x) U_nu(x+K)]^dag
     t = mul_nn(a6, a2);
-    mac_aa(acc, LinkFull<R>::load(Z, K, xpn, V), t);  // (c)
+    mac_aa(acc, LinkFull<R>::load(Z, K, xpn, V), t);
   }
   {
     mat3<R> a3 = U(K, xmk_pn, V);  // U_K(x-K+nu)
     mat3<R> a4 = U(NU, xmk, V);    // U_nu(x-K)
     mat3<R> a5 = U(K, xmk, V);     // U_K(x-K)
+    // (b) = [U_nu(x-K) U_K(x-K+nu)]^dag Z_K(x-K)^dag
     mat3<R> t = mul_nn(a4, a3);
-    mac_aa(acc, t, LinkFull<R>::load(Z, K, xmk, V));  // (b)
+    mac_aa(acc, t, LinkFull<R>::load(Z, K, xmk, V));
+    // (d) + (e) = [Z_K(x+nu-K) U_nu(x-K)^dag + U_K(x-K+nu)^dag Z_nu(x-K)] U_K(x-K)
     t = mul_na(LinkFull<R>::load(Z, K, xmk_pn, V), a4);
-    mac_nn(acc, t, a5);  // (d)
-    t = mul_an(a3, LinkFull<R>::load(Z, NU, xmk, V));
-    mac_nn(acc, t, a5);  // (e)
+    mac_an(t, a3, LinkFull<R>::load(Z, NU, xmk, V));
+    mac_nn(acc, t, a5);
   }
 }
 

@@ -322,10 +322,10 @@ __device__ __forceinline__ float ch_eps<float>() { return 3.0e-8f; }
 template <>
 __device__ __forceinline__ double ch_eps<double>() { return 5.0e-18; }
 
-#define GF_CH_TERMS 40
+#define GF_CH_TERMS 44
 // 1/n! for n = 0 .. GF_CH_TERMS-1
-static __constant__ double c_inv_fact_d[GF_CH_TERMS] = {1.0, 1.0, 0.5, 0.16666666666666666, 0.041666666666666664, 0.008333333333333333, 0.001388888888888889, 0.0001984126984126984, 2.48015873015873e-05, 2.7557319223985893e-06, 2.755731922398589e-07, 2.505210838544172e-08, 2.08767569878681e-09, 1.6059043836821613e-10, 1.1470745597729725e-11, 7.647163731819816e-13, 4.779477332387385e-14, 2.8114572543455206e-15, 1.5619206968586225e-16, 8.22063524662433e-18, 4.110317623312165e-19, 1.9572941063391263e-20, 8.896791392450574e-22, 3.8681701706306835e-23, 1.6117375710961184e-24, 6.446950284384474e-26, 2.4795962632247972e-27, 9.183689863795546e-29, 3.279889237069838e-30, 1.1309962886447718e-31, 3.7699876288159054e-33, 1.2161250415535181e-34, 3.800390754854744e-36, 1.151633562077195e-37, 3.387157535521162e-39, 9.67759295863189e-41, 2.688220266286636e-42, 7.265460179153071e-44, 1.911963205040282e-45, 4.902469756513544e-47};
-static __constant__ float c_inv_fact_f[GF_CH_TERMS] = {1.0f, 1.0f, 0.5f, 0.166666672f, 0.0416666679f, 0.00833333377f, 0.00138888892f, 0.000198412701f, 2.48015876e-05f, 2.75573188e-06f, 2.755732e-07f, 2.50521079e-08f, 2.08767559e-09f, 1.60590444e-10f, 1.14707454e-11f, 7.64716361e-13f, 4.77947726e-14f, 2.81145736e-15f, 1.56192068e-16f, 8.22063508e-18f, 4.11031759e-19f, 1.95729415e-20f, 8.89679096e-22f, 3.8681703e-23f, 1.61173759e-24f, 6.44695034e-26f, 2.47959628e-27f, 9.18368981e-29f, 3.27988916e-30f, 1.13099625e-31f, 3.76998781e-33f, 1.21612501e-34f, 3.80039067e-36f, 1.1516336e-37f, 3.38715699e-39f, 9.67764745e-41f, 2.68769045e-42f, 7.28675201e-44f, 1.40129846e-45f, 0.0f};
+static __constant__ double c_inv_fact_d[GF_CH_TERMS] = {1.0, 1.0, 0.5, 0.16666666666666666, 0.041666666666666664, 0.008333333333333333, 0.001388888888888889, 0.0001984126984126984, 2.48015873015873e-05, 2.7557319223985893e-06, 2.755731922398589e-07, 2.505210838544172e-08, 2.08767569878681e-09, 1.6059043836821613e-10, 1.1470745597729725e-11, 7.647163731819816e-13, 4.779477332387385e-14, 2.8114572543455206e-15, 1.5619206968586225e-16, 8.22063524662433e-18, 4.110317623312165e-19, 1.9572941063391263e-20, 8.896791392450574e-22, 3.8681701706306835e-23, 1.6117375710961184e-24, 6.446950284384474e-26, 2.4795962632247972e-27, 9.183689863795546e-29, 3.279889237069838e-30, 1.1309962886447718e-31, 3.7699876288159054e-33, 1.2161250415535181e-34, 3.800390754854744e-36, 1.151633562077195e-37, 3.387157535521162e-39, 9.67759295863189e-41, 2.688220266286636e-42, 7.265460179153071e-44, 1.911963205040282e-45, 4.902469756513544e-47, 1.225617439128386e-48, 2.9893108271424046e-50, 7.117406731291439e-52, 1.6552108677421951e-53};
+static __constant__ float c_inv_fact_f[GF_CH_TERMS] = {1.0f, 1.0f, 0.5f, 0.166666672f, 0.0416666679f, 0.00833333377f, 0.00138888892f, 0.000198412701f, 2.48015876e-05f, 2.75573188e-06f, 2.755732e-07f, 2.50521079e-08f, 2.08767559e-09f, 1.60590444e-10f, 1.14707454e-11f, 7.64716361e-13f, 4.77947726e-14f, 2.81145736e-15f, 1.56192068e-16f, 8.22063508e-18f, 4.11031759e-19f, 1.95729415e-20f, 8.89679096e-22f, 3.8681703e-23f, 1.61173759e-24f, 6.44695034e-26f, 2.47959628e-27f, 9.18368981e-29f, 3.27988916e-30f, 1.13099625e-31f, 3.76998781e-33f, 1.21612501e-34f, 3.80039067e-36f, 1.1516336e-37f, 3.38715699e-39f, 9.67764745e-41f, 2.68769045e-42f, 7.28675201e-44f, 1.40129846e-45f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
 
 template <typename R>
 __device__ __forceinline__ R inv_fact(int n);
@@ -333,6 +333,52 @@ template <>
 __device__ __forceinline__ double inv_fact<double>(int n) { return c_inv_fact_d[n]; }
 template <>
 __device__ __forceinline__ float inv_fact<float>(int n) { return c_inv_fact_f[n]; }
+
+// One term of the series: advance the power coefficients from Q^{n-1} to
+// Q^n and add i^n/n! times them; the phase i^n is the compile-time PH
+// (0: 1, 1: i, 2: -1, 3: -i), so each term costs adds only.
+template <typename R, bool DERIV, int PH>
+struct ch_state {
+  static __device__ __forceinline__ R step(int n, R c0, R c1, R& a, R& b, R& c, R& a0, R& b0, R& c0d, R& a1, R& b1,
+                                           R& c1d, R* fr, R* fi, R* d1r, R* d1i, R* d2r, R* d2i) {
+    R na = c0 * c, nb = a + c1 * c, nc = b;
+    R na0 = 0, nb0 = 0, nc0 = 0, na1 = 0, nb1 = 0, nc1 = 0;
+    if (DERIV) {
+      na0 = c + c0 * c0d;
+      nb0 = a0 + c1 * c0d;
+      nc0 = b0;
+      na1 = c0 * c1d;
+      nb1 = a1 + c + c1 * c1d;
+      nc1 = b1;
+    }
+    a = na; b = nb; c = nc;
+    const R fact = inv_fact<R>(n);
+    R t[3] = {a * fact, b * fact, c * fact};
+    R mag = fabs(t[0]) + fabs(t[1]) + fabs(t[2]);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      if (PH == 0) fr[j] += t[j];
+      if (PH == 1) fi[j] += t[j];
+      if (PH == 2) fr[j] -= t[j];
+      if (PH == 3) fi[j] -= t[j];
+    }
+    if (DERIV) {
+      a0 = na0; b0 = nb0; c0d = nc0;
+      a1 = na1; b1 = nb1; c1d = nc1;
+      R u0[3] = {a0 * fact, b0 * fact, c0d * fact};
+      R u1[3] = {a1 * fact, b1 * fact, c1d * fact};
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        if (PH == 0) { d2r[j] += u0[j]; d1r[j] += u1[j]; }
+        if (PH == 1) { d2i[j] += u0[j]; d1i[j] += u1[j]; }
+        if (PH == 2) { d2r[j] -= u0[j]; d1r[j] -= u1[j]; }
+        if (PH == 3) { d2i[j] -= u0[j]; d1i[j] -= u1[j]; }
+      }
+      mag += fabs(u0[0]) + fabs(u0[1]) + fabs(u0[2]) + fabs(u1[0]) + fabs(u1[1]) + fabs(u1[2]);
+    }
+    return mag;
+  }
+};
 
 template <typename R, bool DERIV>
 __device__ __forceinline__ void ch_coefficients(R c0, R c1, ch_coef<R>& out) {
@@ -342,42 +388,13 @@ __device__ __forceinline__ void ch_coefficients(R c0, R c1, ch_coef<R>& out) {
   R a1 = 0, b1 = 0, c1d = 0;  // d/dc1
   R fr[3] = {R(1), R(0), R(0)}, fi[3] = {R(0), R(0), R(0)};
   R d1r[3] = {0, 0, 0}, d1i[3] = {0, 0, 0}, d2r[3] = {0, 0, 0}, d2i[3] = {0, 0, 0};
-  for (int n = 1; n < GF_CH_TERMS; ++n) {
-    // advance powers: Q^n from Q^{n-1}
-    R na = c0 * c;
-    R nb = a + c1 * c;
-    R nc = b;
-    R na0 = c + c0 * c0d;
-    R nb0 = a0 + c1 * c0d;
-    R nc0 = b0;
-    R na1 = c0 * c1d;
-    R nb1 = a1 + c + c1 * c1d;
-    R nc1 = b1;
-    a = na; b = nb; c = nc;
-    a0 = na0; b0 = nb0; c0d = nc0;
-    a1 = na1; b1 = nb1; c1d = nc1;
-    const R fact = inv_fact<R>(n);
-    R ta = a * fact, tb = b * fact, tc = c * fact;
-    // i^n: n%4 = 0 -> 1, 1 -> i, 2 -> -1, 3 -> -i
-    int ph = n & 3;
-    R sr = (ph == 0) ? R(1) : ((ph == 2) ? R(-1) : R(0));
-    R si = (ph == 1) ? R(1) : ((ph == 3) ? R(-1) : R(0));
-    fr[0] += sr * ta; fi[0] += si * ta;
-    fr[1] += sr * tb; fi[1] += si * tb;
-    fr[2] += sr * tc; fi[2] += si * tc;
-    R mag = fabs(ta) + fabs(tb) + fabs(tc);
-    if (DERIV) {
-      R ta0 = a0 * fact, tb0 = b0 * fact, tc0 = c0d * fact;
-      R ta1 = a1 * fact, tb1 = b1 * fact, tc1 = c1d * fact;
-      d2r[0] += sr * ta0; d2i[0] += si * ta0;
-      d2r[1] += sr * tb0; d2i[1] += si * tb0;
-      d2r[2] += sr * tc0; d2i[2] += si * tc0;
-      d1r[0] += sr * ta1; d1i[0] += si * ta1;
-      d1r[1] += sr * tb1; d1i[1] += si * tb1;
-      d1r[2] += sr * tc1; d1i[2] += si * tc1;
-      mag += fabs(ta0) + fabs(tb0) + fabs(tc0) + fabs(ta1) + fabs(tb1) + fabs(tc1);
-    }
-    if (n >= 4 && mag < ch_eps<R>()) break;
+  // terms n = 4k+1 .. 4k+4 have phases i, -1, -i, 1
+  for (int n = 1; n + 3 < GF_CH_TERMS; n += 4) {
+    ch_state<R, DERIV, 1>::step(n, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
+    ch_state<R, DERIV, 2>::step(n + 1, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
+    ch_state<R, DERIV, 3>::step(n + 2, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
+    R mag = ch_state<R, DERIV, 0>::step(n + 3, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
+    if (mag < ch_eps<R>()) break;
   }
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
@@ -387,6 +404,32 @@ __device__ __forceinline__ void ch_coefficients(R c0, R c1, ch_coef<R>& out) {
       out.b2[j] = mk(d2r[j], d2i[j]);
     }
   }
+}
+
+// Q^2 of a Hermitian Q: Hermitian, so six entries are computed.
+template <typename R>
+__device__ __forceinline__ mat3<R> herm_square(const mat3<R>& q) {
+  mat3<R> r;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    R d = q.e[i][i].re * q.e[i][i].re;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      if (k != i) d += q.e[i][k].re * q.e[i][k].re + q.e[i][k].im * q.e[i][k].im;
+    r.e[i][i] = mk(d, R(0));
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = i + 1; j < 3; ++j) {
+      // sum_k Q_ik Q_kj with Q_ii, Q_jj real
+      cplx<R> v = q.e[i][i].re * q.e[i][j] + q.e[j][j].re * q.e[i][j];
+      int k = 3 - i - j;
+      fma_(v, q.e[i][k], q.e[k][j]);
+      r.e[i][j] = v;
+      r.e[j][i] = conj(v);
+    }
+  return r;
 }
 
 // c1 = tr(Q^2)/2 and c0 = det(Q) of a traceless Hermitian matrix.
@@ -411,7 +454,7 @@ __device__ __forceinline__ mat3<R> expiq(const mat3<R>& q, mat3<R>* q2out = null
   herm_invariants(q, c0, c1);
   ch_coef<R> cc;
   ch_coefficients<R, false>(c0, c1, cc);
-  mat3<R> q2 = mul_nn(q, q);
+  mat3<R> q2 = herm_square(q);
   mat3<R> e;
 #pragma unroll
   for (int i = 0; i < 3; ++i)
