@@ -373,6 +373,53 @@ def run_reference(args):
     return 0
 
 
+def run_precision_mode(args):
+    """Mixed vs plain fp64 from one thermalised configuration: thermalise with
+    `--therm` mixed trajectories from a Haar start (kept unconditionally), then
+    `--steps` trajectories, each from that same configuration with fresh
+    momenta, in both forms. Reports |dH_mixed - dH_fp64|, the agreement of the
+    Metropolis decisions under the same uniform, and the plaquette difference."""
+    import numpy as np
+    import torch
+    import __graft_entry__ as entry
+    pkg = entry.build()
+    L = args.lattice
+    U, P, drv = make_setup(pkg, L, "mixed", SEED)
+    t0 = time.perf_counter()
+    for t in range(args.therm):
+        pkg.gaussian_momenta_(P, seed=SEED + 11, sweep=t)
+        pkg.md_trajectory_(U, P, drv)
+    t_therm = time.perf_counter() - t0
+    U0 = U.to_host()
+    plaq0 = pkg.measure_plaquette(U)
+    del U, P, drv
+    forms = {f: make_setup(pkg, L, f, SEED) for f in ("fp64", "mixed")}
+    rng = np.random.RandomState(2024)
+    rows = []
+    for i in range(args.steps):
+        u = rng.uniform()
+        r = {}
+        for f, (Uf, Pf, df) in forms.items():
+            Uf.from_host(U0)
+            pkg.gaussian_momenta_(Pf, seed=SEED + 1000, sweep=i)
+            res = pkg.md_trajectory_(Uf, Pf, df)
+            r[f] = (res.delta_hamiltonian, pkg.measure_plaquette(Uf))
+        acc64 = u < np.exp(-r["fp64"][0])
+        accm = u < np.exp(-r["mixed"][0])
+        rows.append({"dH_fp64": r["fp64"][0], "dH_mixed": r["mixed"][0],
+                     "abs_diff": abs(r["mixed"][0] - r["fp64"][0]), "plaq_diff": abs(r["mixed"][1] - r["fp64"][1]),
+                     "same_decision": bool(acc64 == accm)})
+    d = [x["abs_diff"] for x in rows]
+    out = {"mode": "precision", "lattice": [L] * 4, "workload": workload_name(L), "therm": args.therm,
+           "therm_seconds": t_therm, "plaquette_start": plaq0, "trajectories": len(rows),
+           "abs_dH_diff_max": max(d), "abs_dH_diff_median": float(np.median(d)),
+           "same_decision": sum(x["same_decision"] for x in rows),
+           "plaq_diff_max": max(x["plaq_diff"] for x in rows),
+           "dH_fp64_median_abs": float(np.median([abs(x["dH_fp64"]) for x in rows])), "rows": rows}
+    print(json.dumps(out))
+    return 0
+
+
 def run_kernel_mode(args):
     """Small single-family cases for profiler captures: `force` repeats the
     mixed stout force (gf_stout_mom_update), `link` the fp64 link update."""
@@ -407,11 +454,14 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--therm", type=int, default=10, help="thermalisation trajectories before the Delta H check")
-    ap.add_argument("--mode", default="hmc", choices=["hmc", "force", "link"],
-                    help="hmc: the benchmark; force/link: one kernel family, for profiler captures")
+    ap.add_argument("--mode", default="hmc", choices=["hmc", "force", "link", "precision"],
+                    help="hmc: the benchmark; force/link: one kernel family, for profiler captures; "
+                         "precision: mixed vs fp64 Delta H study from one thermalised configuration")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode == "precision":
+        return run_precision_mode(args)
     if args.mode != "hmc":
         return run_kernel_mode(args)
 

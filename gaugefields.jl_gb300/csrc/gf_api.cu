@@ -138,6 +138,7 @@ extern "C" int gf_ctx_destroy(gf_ctx* ctx) {
   field_delete(ctx->w_link32);
   if (ctx->w_stout64) gf_stout_destroy(ctx->w_stout64);
   if (ctx->w_stout32) gf_stout_destroy(ctx->w_stout32);
+  if (ctx->w_stoutdf) gf_stout_destroy(ctx->w_stoutdf);
   if (ctx->d_partials) cudaFree(ctx->d_partials);
   if (ctx->d_result) cudaFree(ctx->d_result);
   if (ctx->h_result) cudaFreeHost(ctx->h_result);
@@ -347,7 +348,8 @@ extern "C" int gf_staple(gf_ctx* ctx, const gf_field* U, int mu, gf_field* V) {
 // ---------------------------------------------------------------------------
 static gf_stout* stout_new(gf_ctx* ctx, int nlev, const double* rho, int precision, int store) {
   need(nlev >= 1 && nlev <= GF_MAX_STOUT, "stout: number of levels must be 1..GF_MAX_STOUT");
-  need(precision == GF_FP64 || precision == GF_MIXED, "stout: precision must be GF_FP64 or GF_MIXED");
+  need(precision == GF_FP64 || precision == GF_MIXED || precision == GF_PREC_DF,
+       "stout: precision must be GF_FP64 or GF_MIXED");
   for (int l = 0; l < nlev; ++l) need(std::isfinite(rho[l]), "stout: rho must be finite");
   gf_stout* st = new gf_stout();
   st->ctx = ctx;
@@ -355,10 +357,14 @@ static gf_stout* stout_new(gf_ctx* ctx, int nlev, const double* rho, int precisi
   for (int l = 0; l < nlev; ++l) st->rho[l] = rho[l];
   st->precision = precision;
   st->store = store ? 1 : 0;
-  int lk = precision == GF_FP64 ? GF_LINK64 : GF_LINK32;
-  int mk = precision == GF_FP64 ? GF_MAT64 : GF_MAT32;
+  int lk = precision == GF_MIXED ? GF_LINK32 : GF_LINK64;
+  int mk = precision == GF_MIXED ? GF_MAT32 : GF_MAT64;
   try {
     for (int l = 1; l <= nlev; ++l) st->lev_in[l] = field_new(ctx, lk);
+    if (precision == GF_PREC_DF) {
+      st->store = 0;  // forward only: no C, no back-propagation buffers
+      return st;
+    }
     if (st->store)
       for (int l = 0; l < nlev; ++l) st->C[l] = field_new(ctx, mk);
     st->Z = field_new(ctx, mk);
@@ -375,6 +381,7 @@ static gf_stout* stout_new(gf_ctx* ctx, int nlev, const double* rho, int precisi
 extern "C" int gf_stout_create(gf_ctx* ctx, int nlev, const double* rho, int precision, int store, gf_stout** out) {
   API_BEGIN
   need(ctx && rho && out, "gf_stout_create: null argument");
+  need(precision == GF_FP64 || precision == GF_MIXED, "gf_stout_create: precision must be GF_FP64 or GF_MIXED");
   *out = stout_new(ctx, nlev, rho, precision, store);
   API_END(ctx)
 }
@@ -439,7 +446,8 @@ static void check_md(const gf_md_params* p) {
 }
 
 static gf_stout* ctx_stout(gf_ctx* ctx, const gf_md_params* p, int precision) {
-  gf_stout** slot = precision == GF_FP64 ? &ctx->w_stout64 : &ctx->w_stout32;
+  gf_stout** slot = precision == GF_FP64 ? &ctx->w_stout64
+                    : (precision == GF_MIXED ? &ctx->w_stout32 : &ctx->w_stoutdf);
   bool same = *slot && (*slot)->nlev == p->nstout;
   if (same)
     for (int l = 0; l < p->nstout; ++l) same = same && (*slot)->rho[l] == p->rho[l];
@@ -451,11 +459,15 @@ static gf_stout* ctx_stout(gf_ctx* ctx, const gf_md_params* p, int precision) {
   return *slot;
 }
 
+// The potential on the (smeared) fp64 links. The plain form computes it in
+// fp64; the mixed form in double-float arithmetic (~1e-14 per operation) on
+// the fp32 pipes, with fp64 storage and fp64 global sums.
 static double potential(gf_ctx* ctx, const gf_field* U, const gf_md_params* p) {
-  if (p->nstout == 0) return -(p->beta / 3.0) * plaquette_sum(ctx, U);
-  gf_stout* st = ctx_stout(ctx, p, GF_FP64);
+  bool df = p->precision == GF_MIXED;
+  if (p->nstout == 0) return -(p->beta / 3.0) * plaquette_sum(ctx, U, df);
+  gf_stout* st = ctx_stout(ctx, p, df ? GF_PREC_DF : GF_FP64);
   stout_forward(ctx, st, U, nullptr);
-  return -(p->beta / 3.0) * plaquette_sum(ctx, stout_top(st));
+  return -(p->beta / 3.0) * plaquette_sum(ctx, stout_top(st), df);
 }
 
 static double hamiltonian(gf_ctx* ctx, const gf_field* U, const gf_field* P, const gf_md_params* p) {
@@ -482,7 +494,9 @@ static void mom_update(gf_ctx* ctx, gf_field* P, const gf_field* U, const gf_fie
 // saves one fp64 stout forward + plaquette per trajectory; any change of the
 // links changes the hash, so a reused value is bitwise the recomputed one.
 static bool vcache_hit(const gf_ctx* ctx, const gf_md_params* p, unsigned long long h) {
-  if (!ctx->vc_valid || ctx->vc_hash != h || ctx->vc_beta != p->beta || ctx->vc_nstout != p->nstout) return false;
+  if (!ctx->vc_valid || ctx->vc_hash != h || ctx->vc_beta != p->beta || ctx->vc_nstout != p->nstout ||
+      ctx->vc_precision != p->precision)
+    return false;
   for (int l = 0; l < p->nstout; ++l)
     if (ctx->vc_rho[l] != p->rho[l]) return false;
   return true;
@@ -494,6 +508,7 @@ static void vcache_set(gf_ctx* ctx, const gf_md_params* p, unsigned long long h,
   ctx->vc_V = V;
   ctx->vc_beta = p->beta;
   ctx->vc_nstout = p->nstout;
+  ctx->vc_precision = p->precision;
   for (int l = 0; l < GF_MAX_STOUT; ++l) ctx->vc_rho[l] = l < p->nstout ? p->rho[l] : 0.0;
 }
 
@@ -521,16 +536,17 @@ static MDResult md_run(gf_ctx* ctx, gf_field* U, gf_field* P, const gf_md_params
   // _md_fast_qpq! does (molecular_dynamics.jl:618-633): n+1 link updates and
   // n forces (QPQ), or n+1 forces and n link updates (PQP). The trajectory
   // is the one of md_step! up to rounding.
+  const bool df = p->precision == GF_MIXED;  // link updates in double-float
   if (p->integrator == GF_QPQ) {
-    link_update(ctx, U, P, 0.5 * eps, p->reunitarize, U32);
+    link_update(ctx, U, P, 0.5 * eps, p->reunitarize, U32, df);
     for (int n = 0; n < p->steps; ++n) {
       mom_update(ctx, P, U, U32, eps, p);
-      link_update(ctx, U, P, (n == p->steps - 1) ? 0.5 * eps : eps, p->reunitarize, U32);
+      link_update(ctx, U, P, (n == p->steps - 1) ? 0.5 * eps : eps, p->reunitarize, U32, df);
     }
   } else {
     mom_update(ctx, P, U, U32, 0.5 * eps, p);
     for (int n = 0; n < p->steps; ++n) {
-      link_update(ctx, U, P, eps, p->reunitarize, U32);
+      link_update(ctx, U, P, eps, p->reunitarize, U32, df);
       mom_update(ctx, P, U, U32, (n == p->steps - 1) ? 0.5 * eps : eps, p);
     }
   }

@@ -33,6 +33,10 @@ void count_launch();
 
 #define GF_PROF_CAP 4096
 
+// Internal stack precision: fp64 storage with double-float arithmetic (the
+// mixed form's Hamiltonian); never accepted from the C-ABI.
+#define GF_PREC_DF 2
+
 struct gf_field {
   gf_ctx* ctx;
   int kind;
@@ -59,6 +63,7 @@ struct gf_ctx {
   gf_field* w_link32;     // fp32 12-real shadow of the thin links (mixed form)
   gf_stout* w_stout64;    // stout workspace, fp64
   gf_stout* w_stout32;    // stout workspace, fp32
+  gf_stout* w_stoutdf;    // stout forward for the mixed form's Hamiltonian (double-float)
   int w_stout_nlev;
   double w_stout_rho[GF_MAX_STOUT];
   // potential of the last configuration an MD call ended on, keyed by a
@@ -68,7 +73,7 @@ struct gf_ctx {
   int vc_valid;
   unsigned long long vc_hash;
   double vc_V, vc_beta;
-  int vc_nstout;
+  int vc_nstout, vc_precision;
   double vc_rho[GF_MAX_STOUT];
   // per-kernel CUDA-event timing on the context's stream (gf_prof_*)
   int prof_on;
@@ -137,7 +142,7 @@ void mom_axpy(gf_ctx* ctx, gf_field* y, double a, const gf_field* x);  // y += a
 void mom_scale(gf_ctx* ctx, gf_field* y, double a);                      // y *= a
 
 // ---- Wilson action pieces (gf_wilson.cu) ----
-double plaquette_sum(gf_ctx* ctx, const gf_field* U);  // sum_x sum_{mu<nu} Re tr P
+double plaquette_sum(gf_ctx* ctx, const gf_field* U, bool df = false);  // sum_x sum_{mu<nu} Re tr P
 void staple_up(gf_ctx* ctx, const gf_field* U, int mu, gf_field* V);  // construct_staple! (mu field slot)
 // P <- keep * P + coef * TA-coefficients(U_mu * S_mu), S = sum of the six
 // staples (dS/dU order); keep = 0 overwrites P without reading it.
@@ -145,7 +150,9 @@ void wilson_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double coef,
 
 // ---- link update (gf_update.cu) ----
 // U <- exp(i eps P) U, optional re-unitarisation, optional fp32 shadow copy.
-void link_update(gf_ctx* ctx, gf_field* U, const gf_field* P, double eps, int reunit, gf_field* shadow32);
+// df: double-float arithmetic on the fp32 pipes (the mixed form), else fp64.
+void link_update(gf_ctx* ctx, gf_field* U, const gf_field* P, double eps, int reunit, gf_field* shadow32,
+                 bool df = false);
 void exp_mom_links(gf_ctx* ctx, gf_field* W, const gf_field* P, double a, const gf_field* U);  // W = exp(i a P) U
 void reunitarize_links(gf_ctx* ctx, gf_field* U);
 void link64_to_32(gf_ctx* ctx, gf_field* dst, const gf_field* src);

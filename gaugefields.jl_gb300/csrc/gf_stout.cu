@@ -20,6 +20,7 @@
 // and momentum update at the bottom level).
 #include "gf_internal.h"
 #include "stencil.cuh"
+#include <type_traits>
 
 namespace gf {
 
@@ -48,6 +49,18 @@ struct Prec<float> {
   }
 };
 
+// fp64 storage, double-float arithmetic: forward only (the mixed form's
+// Hamiltonian smears in this precision)
+template <>
+struct Prec<dfl> {
+  typedef LinkSrc<dfl, false> Src;
+  typedef double2 LinkElem;
+  typedef double2 MatElem;
+  static __device__ __forceinline__ void store_link(double2* p, int mu, int s, int V, const mat3<dfl>& m) {
+    LinkFull<dfl>::store(p, mu, s, V, m);
+  }
+};
+
 // i * r * A  (elementwise)
 template <typename R>
 __device__ __forceinline__ mat3<R> times_i(R r, const mat3<R>& a) {
@@ -66,8 +79,8 @@ template <typename R>
 __global__ void __launch_bounds__(128)
     k_stout_fwd(typename Prec<R>::Src U, typename Prec<R>::LinkElem* __restrict__ Uout,
                 typename Prec<R>::MatElem* __restrict__ Cout, Geom g, R rho) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  int mu = blockIdx.y;
+  int s, mu;
+  link_of_block(s, mu);
   if (s >= g.vol) return;
   const int V = g.vol;
   Site st = site_of(g, s);
@@ -89,8 +102,8 @@ __global__ void __launch_bounds__(128)
     k_bwd_local(typename Prec<R>::Src U, typename Prec<R>::Src Utop, const typename Prec<R>::MatElem* __restrict__ Dbar,
                 const typename Prec<R>::MatElem* __restrict__ Cst, typename Prec<R>::MatElem* __restrict__ Zout,
                 typename Prec<R>::MatElem* __restrict__ Dpout, Geom g, R rho, R halfbeta) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  int mu = blockIdx.y;
+  int s, mu;
+  link_of_block(s, mu);
   if (s >= g.vol) return;
   const int V = g.vol;
   Site st = site_of(g, s);
@@ -203,8 +216,8 @@ __global__ void __launch_bounds__(128)
     k_bwd_gather(typename Prec<R>::Src U, const typename Prec<R>::MatElem* __restrict__ Z,
                  const typename Prec<R>::MatElem* __restrict__ Dp, typename Prec<R>::MatElem* __restrict__ Dout,
                  double* __restrict__ P, Geom g, R rho, double coef) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  int nu = blockIdx.y;
+  int s, nu;
+  link_of_block(s, nu);
   if (s >= g.vol) return;
   const int V = g.vol;
   Site st = site_of(g, s);
@@ -242,9 +255,10 @@ static typename Prec<R>::Src src_of(const gf_field* f) {
 
 template <typename R>
 static void forward_impl(gf_ctx* ctx, gf_stout* st) {
-  dim3 grid(blocks_for(ctx->geom.vol, 128), 4);
+  dim3 grid(4 * blocks_for(ctx->geom.vol, 128));
   for (int l = 0; l < st->nlev; ++l) {
-    ProfScope prof(ctx, sizeof(R) == 8 ? GF_K_STOUT_FWD64 : GF_K_STOUT_FWD);
+    ProfScope prof(ctx, std::is_same<R, float>::value ? GF_K_STOUT_FWD
+                        : (std::is_same<R, double>::value ? GF_K_STOUT_FWD64 : GF_K_STOUT_FWD_DF));
     k_stout_fwd<R><<<grid, 128, 0, ctx->stream>>>(
         src_of<R>(st->lev_in[l]), (typename Prec<R>::LinkElem*)st->lev_in[l + 1]->ptr,
         st->store ? (typename Prec<R>::MatElem*)st->C[l]->ptr : nullptr, ctx->geom, (R)st->rho[l]);
@@ -253,7 +267,7 @@ static void forward_impl(gf_ctx* ctx, gf_stout* st) {
 }
 
 void stout_forward(gf_ctx* ctx, gf_stout* st, const gf_field* U, gf_field* Uout) {
-  int lk = st->precision == GF_FP64 ? GF_LINK64 : GF_LINK32;
+  int lk = st->precision == GF_MIXED ? GF_LINK32 : GF_LINK64;
   gf_field* old = st->lev_in[0];
   if (U->kind == lk) {
     // alias the caller's thin links (not owned by the stack)
@@ -261,7 +275,7 @@ void stout_forward(gf_ctx* ctx, gf_stout* st, const gf_field* U, gf_field* Uout)
     a->owned = 0;
     st->lev_in[0] = a;
     field_delete(old);  // frees storage only if the old entry was owned
-  } else if (st->precision != GF_FP64 && U->kind == GF_LINK64) {
+  } else if (st->precision == GF_MIXED && U->kind == GF_LINK64) {
     // mixed stack fed with fp64 links: keep an owned fp32 12-real thin copy
     if (!old || !old->owned) {
       st->lev_in[0] = field_new(ctx, GF_LINK32);
@@ -272,6 +286,7 @@ void stout_forward(gf_ctx* ctx, gf_stout* st, const gf_field* U, gf_field* Uout)
     throw gf_error(GF_EINVAL, "stout forward: link field kind does not match the stack precision");
   }
   if (st->precision == GF_FP64) forward_impl<double>(ctx, st);
+  else if (st->precision == GF_PREC_DF) forward_impl<dfl>(ctx, st);
   else forward_impl<float>(ctx, st);
   st->have_forward = 1;
   if (Uout) copy_field(ctx, Uout, st->lev_in[st->nlev]);
@@ -282,7 +297,7 @@ const gf_field* stout_top(const gf_stout* st) { return st->lev_in[st->nlev]; }
 template <typename R>
 static void backward_impl(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, double beta, gf_field* dSdU,
                           gf_field* P, double eps) {
-  dim3 grid(blocks_for(ctx->geom.vol, 128), 4);
+  dim3 grid(4 * blocks_for(ctx->geom.vol, 128));
   typedef typename Prec<R>::MatElem ME;
   const ME* dbar = dSdUbar ? (const ME*)dSdUbar->ptr : nullptr;
   int cur = 0;
@@ -323,6 +338,7 @@ static void backward_impl(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, do
 void stout_backward(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, double beta, gf_field* dSdU, gf_field* P,
                     double eps) {
   if (!st->have_forward) throw gf_error(GF_ESTATE, "stout backward called before forward");
+  if (st->precision == GF_PREC_DF) throw gf_error(GF_EINVAL, "stout backward: forward-only stack");
   if (st->nlev < 1) throw gf_error(GF_EINVAL, "stout backward needs at least one level");
   int mk = st->precision == GF_FP64 ? GF_MAT64 : GF_MAT32;
   if (dSdUbar && dSdUbar->kind != mk) throw gf_error(GF_EINVAL, "stout backward: dS/dUbar kind does not match the stack precision");

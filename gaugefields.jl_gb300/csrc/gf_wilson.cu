@@ -21,11 +21,14 @@ __global__ void __launch_bounds__(128) k_plaquette(SRC U, Geom g, double* __rest
   block_partial_sum(v, part);
 }
 
-double plaquette_sum(gf_ctx* ctx, const gf_field* U) {
+double plaquette_sum(gf_ctx* ctx, const gf_field* U, bool df) {
   int V = ctx->geom.vol;
   int nb = blocks_for(V, 128);
   ProfScope prof(ctx, GF_K_PLAQ);
-  if (U->kind == GF_LINK64 || U->kind == GF_MAT64) {
+  if (df && U->kind == GF_LINK64) {
+    LinkSrc<dfl, false> src{(const double2*)U->ptr};
+    k_plaquette<dfl><<<nb, 128, 0, ctx->stream>>>(src, ctx->geom, ctx->d_partials);
+  } else if (U->kind == GF_LINK64 || U->kind == GF_MAT64) {
     Src64 src{(const double2*)U->ptr};
     k_plaquette<double><<<nb, 128, 0, ctx->stream>>>(src, ctx->geom, ctx->d_partials);
   } else if (U->kind == GF_LINK32) {
@@ -77,8 +80,8 @@ void staple_up(gf_ctx* ctx, const gf_field* U, int mu, gf_field* Vout) {
 //  * add_force! flow:  coef = factor
 template <typename R, class SRC>
 __global__ void __launch_bounds__(128) k_force_ta(SRC U, double* __restrict__ P, Geom g, double coef, double keep) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  int mu = blockIdx.y;
+  int s, mu;
+  link_of_block(s, mu);
   if (s >= g.vol) return;
   Site st = site_of(g, s);
   const int V = g.vol;
@@ -96,7 +99,7 @@ __global__ void __launch_bounds__(128) k_force_ta(SRC U, double* __restrict__ P,
 
 void wilson_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double coef, double keep) {
   if (P->kind != GF_MOM64) throw gf_error(GF_EINVAL, "force: output must be MOM64");
-  dim3 grid(blocks_for(ctx->geom.vol, 128), 4);
+  dim3 grid(4 * blocks_for(ctx->geom.vol, 128));
   ProfScope prof(ctx, GF_K_FORCE);
   if (U->kind == GF_LINK64) {
     Src64 src{(const double2*)U->ptr};

@@ -75,6 +75,16 @@ GF_HD int nbr2(const Geom& g, const Site& st, int d0, int d1) {
   return eo_of_lex(g, lex, st.par);
 }
 
+// Stencil kernels run one thread per link on a 1-D grid of 4 * ceil(V/bs)
+// blocks; block b handles direction b % 4 of the sites of block b / 4, so the
+// four directions of the same sites run back to back and their shared
+// neighbour links are served from L2 instead of being re-read from HBM once
+// per direction.
+__device__ __forceinline__ void link_of_block(int& s, int& mu) {
+  mu = blockIdx.x & 3;
+  s = (blockIdx.x >> 2) * blockDim.x + threadIdx.x;
+}
+
 // ---------------------------------------------------------------------------
 // Field accessors. `V` is the site count, `s` the even/odd site index.
 // ---------------------------------------------------------------------------
@@ -118,6 +128,28 @@ struct LinkFull<float> {
     float2* b = p + (size_t)mu * 9 * V + s;
 #pragma unroll
     for (int k = 0; k < 9; ++k) b[(size_t)k * V] = make_float2(m.e[k / 3][k % 3].re, m.e[k / 3][k % 3].im);
+  }
+};
+
+// fp64 storage, double-float arithmetic (the mixed form's fp64-class kernels)
+template <>
+struct LinkFull<dfl> {
+  typedef double2 elem;
+  static __device__ __forceinline__ mat3<dfl> load(const double2* __restrict__ p, int mu, int s, int V) {
+    mat3<dfl> m;
+    const double2* b = p + (size_t)mu * 9 * V + s;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      double2 v = __ldg(b + (size_t)k * V);
+      m.e[k / 3][k % 3] = mk(df_from_double(v.x), df_from_double(v.y));
+    }
+    return m;
+  }
+  static __device__ __forceinline__ void store(double2* __restrict__ p, int mu, int s, int V, const mat3<dfl>& m) {
+    double2* b = p + (size_t)mu * 9 * V + s;
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
+      b[(size_t)k * V] = make_double2(df_to_double(m.e[k / 3][k % 3].re), df_to_double(m.e[k / 3][k % 3].im));
   }
 };
 

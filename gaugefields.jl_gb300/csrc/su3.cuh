@@ -12,6 +12,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
+#include "dfloat.cuh"
 
 #define GF_HD __host__ __device__ __forceinline__
 
@@ -327,12 +328,64 @@ __device__ __forceinline__ double ch_eps<double>() { return 5.0e-18; }
 static __constant__ double c_inv_fact_d[GF_CH_TERMS] = {1.0, 1.0, 0.5, 0.16666666666666666, 0.041666666666666664, 0.008333333333333333, 0.001388888888888889, 0.0001984126984126984, 2.48015873015873e-05, 2.7557319223985893e-06, 2.755731922398589e-07, 2.505210838544172e-08, 2.08767569878681e-09, 1.6059043836821613e-10, 1.1470745597729725e-11, 7.647163731819816e-13, 4.779477332387385e-14, 2.8114572543455206e-15, 1.5619206968586225e-16, 8.22063524662433e-18, 4.110317623312165e-19, 1.9572941063391263e-20, 8.896791392450574e-22, 3.8681701706306835e-23, 1.6117375710961184e-24, 6.446950284384474e-26, 2.4795962632247972e-27, 9.183689863795546e-29, 3.279889237069838e-30, 1.1309962886447718e-31, 3.7699876288159054e-33, 1.2161250415535181e-34, 3.800390754854744e-36, 1.151633562077195e-37, 3.387157535521162e-39, 9.67759295863189e-41, 2.688220266286636e-42, 7.265460179153071e-44, 1.911963205040282e-45, 4.902469756513544e-47, 1.225617439128386e-48, 2.9893108271424046e-50, 7.117406731291439e-52, 1.6552108677421951e-53};
 static __constant__ float c_inv_fact_f[GF_CH_TERMS] = {1.0f, 1.0f, 0.5f, 0.166666672f, 0.0416666679f, 0.00833333377f, 0.00138888892f, 0.000198412701f, 2.48015876e-05f, 2.75573188e-06f, 2.755732e-07f, 2.50521079e-08f, 2.08767559e-09f, 1.60590444e-10f, 1.14707454e-11f, 7.64716361e-13f, 4.77947726e-14f, 2.81145736e-15f, 1.56192068e-16f, 8.22063508e-18f, 4.11031759e-19f, 1.95729415e-20f, 8.89679096e-22f, 3.8681703e-23f, 1.61173759e-24f, 6.44695034e-26f, 2.47959628e-27f, 9.18368981e-29f, 3.27988916e-30f, 1.13099625e-31f, 3.76998781e-33f, 1.21612501e-34f, 3.80039067e-36f, 1.1516336e-37f, 3.38715699e-39f, 9.67764745e-41f, 2.68769045e-42f, 7.28675201e-44f, 1.40129846e-45f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
 
+// 1/n! as double-float pairs (hi, lo)
+static __constant__ float c_inv_fact_df[2 * GF_CH_TERMS] = {
+    1.000000000e+00f, 0.000000000e+00f,
+    1.000000000e+00f, 0.000000000e+00f,
+    5.000000000e-01f, 0.000000000e+00f,
+    1.666666716e-01f, -4.967053879e-09f,
+    4.166666791e-02f, -1.241763470e-09f,
+    8.333333768e-03f, -4.346172033e-10f,
+    1.388888923e-03f, -3.363109444e-11f,
+    1.984127011e-04f, -2.725596875e-12f,
+    2.480158764e-05f, -3.406996094e-13f,
+    2.755731884e-06f, 3.793571224e-14f,
+    2.755731998e-07f, -7.575112209e-15f,
+    2.505210794e-08f, 4.417623045e-16f,
+    2.087675588e-09f, 1.108283981e-16f,
+    1.605904437e-10f, -5.352526512e-18f,
+    1.147074536e-11f, 2.372207689e-19f,
+    7.647163610e-13f, 1.220071047e-20f,
+    4.779477256e-14f, 7.625444044e-22f,
+    2.811457359e-15f, -1.046208474e-22f,
+    1.561920681e-16f, 1.540447147e-24f,
+    8.220635078e-18f, 1.681478097e-25f,
+    4.110317591e-19f, 3.237511733e-27f,
+    1.957294152e-20f, -4.612945514e-28f,
+    8.896790960e-22f, 4.328837203e-29f,
+    3.868170298e-23f, -1.273340432e-30f,
+    1.611737591e-24f, -2.018664841e-32f,
+    6.446950340e-26f, -5.609469144e-34f,
+    2.479596285e-27f, -2.157488154e-35f,
+    9.183689810e-29f, 5.383816950e-37f,
+    3.279889164e-30f, 7.296480389e-38f,
+    1.130996247e-31f, 4.137399577e-39f,
+    3.769987809e-33f, -1.804494071e-40f,
+    1.216125015e-34f, 2.696098245e-42f,
+    3.800390671e-36f, 8.407790786e-44f,
+    1.151633601e-37f, -4.203895393e-45f,
+    3.387156991e-39f, 0.000000000e+00f,
+    9.677647454e-41f, -0.000000000e+00f,
+    2.687690455e-42f, 0.000000000e+00f,
+    7.286752014e-44f, -0.000000000e+00f,
+    1.401298464e-45f, 0.000000000e+00f,
+    0.000000000e+00f, 0.000000000e+00f,
+    0.000000000e+00f, 0.000000000e+00f,
+    0.000000000e+00f, 0.000000000e+00f,
+    0.000000000e+00f, 0.000000000e+00f,
+    0.000000000e+00f, 0.000000000e+00f};
+
+template <>
+__device__ __forceinline__ dfl ch_eps<dfl>() { return dfl(2.0e-16f); }
+
 template <typename R>
 __device__ __forceinline__ R inv_fact(int n);
 template <>
 __device__ __forceinline__ double inv_fact<double>(int n) { return c_inv_fact_d[n]; }
 template <>
 __device__ __forceinline__ float inv_fact<float>(int n) { return c_inv_fact_f[n]; }
+template <>
+__device__ __forceinline__ dfl inv_fact<dfl>(int n) { return dfl(c_inv_fact_df[2 * n], c_inv_fact_df[2 * n + 1]); }
 
 // One term of the series: advance the power coefficients from Q^{n-1} to
 // Q^n and add i^n/n! times them; the phase i^n is the compile-time PH

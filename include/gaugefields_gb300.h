@@ -217,7 +217,9 @@ int gf_plaquette_noalloc(const void* links, const int L[4], double* out, void* s
 #define GF_K_BWD_LOCAL64 7
 #define GF_K_BWD_GATHER64 8
 #define GF_K_OTHER 9        /* starts, conversions, kinetic, copies */
-#define GF_K_COUNT 10
+#define GF_K_LINK_UPDATE_DF 10  /* link update in double-float (mixed form) */
+#define GF_K_STOUT_FWD_DF 11    /* stout forward in double-float (mixed-form Hamiltonian) */
+#define GF_K_COUNT 12
 /* Enable (on != 0) or disable CUDA-event timing of every kernel launch on the
  * context's stream; enabling clears the accumulators. */
 int gf_prof_enable(gf_ctx* ctx, int on);

@@ -327,9 +327,59 @@ def test_mixed_precision_trajectory_delta_h(pkg):
     # Same start and momenta: the fp64 Hamiltonian at the start is identical;
     # the fp32 force changes Delta H by a random walk of its rounding errors.
     # On this unthermalised hot start (Delta H ~ 130) the bound is relative.
-    assert results["mixed"].initial_hamiltonian == results["fp64"].initial_hamiltonian
+    h0 = results["fp64"].initial_hamiltonian
+    assert abs(results["mixed"].initial_hamiltonian - h0) <= 1e-12 * abs(h0)
     d64 = results["fp64"].delta_hamiltonian
     assert abs(results["mixed"].delta_hamiltonian - d64) < 1e-4 * max(1.0, abs(d64))
+
+
+def _smeared(pkg, U, beta, prec, steps=10):
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, beta / 2, "plaquette")
+    net = pkg.stout_smearing(U, rho=0.1)
+    pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
+    return pkg.md_driver(U, action, steps=steps, smearing=net, precision=prec)
+
+
+def test_double_float_link_updates_match_fp64(pkg):
+    """The mixed form updates links in double-float arithmetic. With beta = 0
+    the force vanishes, so a trajectory is 11 link updates with constant
+    momenta and the two forms differ only by that arithmetic."""
+    out = {}
+    for prec in ("fp64", "mixed"):
+        U = pkg.gauge_configuration(L8, start="hot", seed=3)
+        P = pkg.gaussian_momenta(U, seed=4)
+        res = pkg.md_trajectory_(U, P, _smeared(pkg, U, 0.0, prec))
+        out[prec] = (U.to_host(), P.to_host(), res)
+    assert frob_links(out["mixed"][0], out["fp64"][0]) < 1e-12
+    assert np.array_equal(out["mixed"][1], out["fp64"][1])
+    assert abs(out["mixed"][2].delta_hamiltonian - out["fp64"][2].delta_hamiltonian) < 1e-9
+
+
+def test_double_float_hamiltonian_matches_fp64(pkg):
+    U = pkg.gauge_configuration(L8, start="hot", seed=5)
+    P = pkg.gaussian_momenta(U, seed=6)
+    h = {prec: pkg.md_hamiltonian(U, P, _smeared(pkg, U, 6.0, prec)) for prec in ("fp64", "mixed")}
+    assert abs(h["mixed"] - h["fp64"]) <= 1e-13 * abs(h["fp64"])
+
+
+def test_potential_reuse_is_bitwise_identical(pkg):
+    """A trajectory that starts where the previous one ended reuses that
+    potential (keyed by a hash of the links); the result equals a fresh run."""
+    U = pkg.gauge_configuration(L4, start="hot", seed=12)
+    P = pkg.gaussian_momenta(U, seed=1)
+    drv = _smeared(pkg, U, 6.0, "fp64", steps=4)
+    r1 = pkg.md_trajectory_(U, P, drv)
+    Uh = U.to_host()
+    pkg.gaussian_momenta_(P, seed=2)
+    r2 = pkg.md_trajectory_(U, P, drv)            # starts from the cached potential
+    V = pkg.gauge_configuration(L4, start="cold")
+    V.from_host(Uh)
+    Q = pkg.gaussian_momenta(V, seed=2)
+    r3 = pkg.md_trajectory_(V, Q, _smeared(pkg, V, 6.0, "fp64", steps=4))  # fresh context
+    assert r2.initial_hamiltonian == r3.initial_hamiltonian
+    assert r2.delta_hamiltonian == r3.delta_hamiltonian
+    assert r2.initial_hamiltonian - r1.final_hamiltonian != 0.0  # new momenta
 
 
 def test_flow(pkg, oracle):
