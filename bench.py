@@ -43,14 +43,21 @@ def workload_name(L):
 # each input field read once, each output written once). fp32 12-real link =
 # 48 B, fp32 3x3 matrix = 72 B, fp64 link = 144 B, fp64 momenta = 64 B.
 # ---------------------------------------------------------------------------
+def _base(kclass):
+    for suf in ("64", "_df"):
+        if kclass.endswith(suf):
+            return kclass[: -len(suf)]
+    return kclass
+
+
 def algorithmic_bytes_per_link(kclass):
     """Compulsory bytes per link of one launch of a kernel class."""
-    fp64 = kclass.endswith("64") or kclass in ("link_update", "plaquette")
+    fp64 = kclass.endswith("64") or kclass.endswith("_df") or kclass in ("link_update", "plaquette")
     link, mat = (144, 144) if fp64 else (48, 72)
-    base = kclass[:-2] if kclass.endswith("64") else kclass
+    base = _base(kclass)
     return {
-        # U in, Ubar out, C out
-        "stout_fwd": link + link + mat,
+        # U in, Ubar out, C out (the double-float forward of the Hamiltonian stores no C)
+        "stout_fwd": link + link + (0 if kclass.endswith("_df") else mat),
         # U, C, Dbar in (top level: Ubar_top in); Z, Dp out -- mean of the two levels
         "bwd_local": (link + mat + mat + 2 * mat + link + mat + link + 2 * mat) / 2.0,
         # U, Z, Dp in; D out (upper level) or P read+write (bottom level) -- mean
@@ -67,7 +74,7 @@ def algorithmic_flops_per_link(kclass):
     """3x3 complex products counted at 198 flops (216 when accumulated)."""
     mm, mac, rec = 198, 216, 42
     staples = 6 * (mm + mac)  # six staples, two products each
-    base = kclass[:-2] if kclass.endswith("64") else kclass
+    base = _base(kclass)
     return {
         "stout_fwd": staples + 2 * mm + 600,             # + U S, exp (series + Qh^2), E U
         "bwd_local": (staples / 2.0) + 8 * mm + 900,     # mean: top level rebuilds staples
@@ -420,6 +427,67 @@ def run_precision_mode(args):
     return 0
 
 
+def run_wilson_mode(args):
+    """Plain fp64 Wilson HMC at scale: cold start, beta = 6.0, tau = 1, 20 QPQ
+    steps, `--steps` seeded trajectories (after `--warmup`), then the RK3 Wilson
+    flow with eps = 0.01 to t = 2 on the final configuration, recording the
+    plaquette-defined E(t) = 36 (1 - <P>) after every flow step."""
+    import numpy as np
+    import torch
+    import ctypes
+    import __graft_entry__ as entry
+    pkg = entry.build()
+    from gaugefields_gb300 import _lib
+    lib = _lib.load()
+    L = args.lattice
+    V = L ** 4
+    U = pkg.gauge_configuration((L,) * 4, start="cold")
+    P = pkg.gauge_momenta(U)
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, 3.0, "plaquette")
+    drv = pkg.md_driver(U, action, steps=NSTEPS, trajectory_length=TAU)
+    stream = torch.cuda.Stream()
+    U.ctx.set_stream(stream.cuda_stream)
+    U.ctx.torch_stream = stream
+    rng = np.random.RandomState(1234)
+    for t in range(args.warmup):
+        pkg.hmc_update_(U, P, drv, seed=1234, sweep=t, unif=rng.uniform())
+    lib.gf_prof_enable(U.ctx.h, 1)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    acc = 0
+    for t in range(args.steps):
+        acc += pkg.hmc_update_(U, P, drv, seed=1234, sweep=args.warmup + t, unif=rng.uniform()).accepted
+    e.record(stream)
+    torch.cuda.synchronize()
+    sec = s.elapsed_time(e) / 1e3
+    ms, cnt = ctypes.c_double(), ctypes.c_longlong()
+    lib.gf_prof_read(U.ctx.h, _lib.KERNEL_CLASSES.index("force"), ctypes.byref(ms), ctypes.byref(cnt))
+    force_ms = ms.value / max(1, cnt.value)
+    lib.gf_prof_enable(U.ctx.h, 0)
+    # the staple/force kernel reads U (4 x 144 B) and P (4 x 64 B) and writes P per site
+    force_bytes = 4 * V * (144 + 64 + 64)
+    plaq = pkg.measure_plaquette(U)
+    g = pkg.Gradientflow(U, Nflow=1, eps=0.01)
+    E = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(200):
+        pkg.flow_(U, g)
+        E.append(36.0 * (1.0 - pkg.measure_plaquette(U)))
+    flow_sec = time.perf_counter() - t0
+    link_updates = 4 * V * (NSTEPS + 1) * args.steps
+    out = {"mode": "wilson", "lattice": [L] * 4, "workload": "%d^4 cold start, fp64 Wilson HMC beta=6.0, tau=1, "
+           "20 QPQ steps; RK3 flow eps=0.01 to t=2" % L, "trajectories": args.steps, "traj_per_s": args.steps / sec,
+           "link_updates_per_s": link_updates / sec, "accepted": acc, "plaquette": plaq,
+           "force_kernel": {"avg_ms": force_ms, "algorithmic_GBps": force_bytes / force_ms / 1e6},
+           "flow_steps_per_s": 200 / flow_sec, "E_t": [[round(0.01 * (k + 1), 2), E[k]] for k in range(0, 200, 20)],
+           "t2E_at_t2": 4.0 * E[-1]}
+    print(json.dumps(out))
+    return 0
+
+
 def run_kernel_mode(args):
     """Small single-family cases for profiler captures: `force` repeats the
     mixed stout force (gf_stout_mom_update), `link` the fp64 link update."""
@@ -454,7 +522,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--therm", type=int, default=10, help="thermalisation trajectories before the Delta H check")
-    ap.add_argument("--mode", default="hmc", choices=["hmc", "force", "link", "precision"],
+    ap.add_argument("--mode", default="hmc", choices=["hmc", "force", "link", "precision", "wilson"],
                     help="hmc: the benchmark; force/link: one kernel family, for profiler captures; "
                          "precision: mixed vs fp64 Delta H study from one thermalised configuration")
     args = ap.parse_args()
@@ -462,6 +530,8 @@ def main():
         return run_reference(args)
     if args.mode == "precision":
         return run_precision_mode(args)
+    if args.mode == "wilson":
+        return run_wilson_mode(args)
     if args.mode != "hmc":
         return run_kernel_mode(args)
 
@@ -519,11 +589,12 @@ def main():
                 "frac": achieved / hbm_peak, "peak_note": hbm_note, "algorithmic_bytes_per_launch": alg_bytes,
                 "traffic": read_traffic(dom, L), "launches": d["launches"], "avg_launch_ms": 1e3 * per_launch_s}
         fl = algorithmic_flops_per_link(dom) * 4 * V
-        pk = peaks["fp64_tflops"] if prec == "fp64" else peaks["fp32_tflops"]
+        pk = peaks["fp32_tflops"] if prec == "fp32" else peaks["fp64_tflops"]
+        note = {"fp64": "cuBLAS dgemm measured in this run", "fp32": "cuBLAS sgemm (no TF32) measured in this run",
+                "df": "double-float flops (fp64-class) against the cuBLAS dgemm rate measured in this run"}[prec]
         compute = {"kernel": dom, "precision": prec, "achieved_tflops": fl / per_launch_s / 1e12, "peak_tflops": pk,
-                   "peak_note": "cuBLAS %s measured in this run" % ("dgemm" if prec == "fp64" else "sgemm (no TF32)"),
-                   "flops_per_launch": fl, "frac": fl / per_launch_s / 1e12 / pk,
-                   "binding": "fp64 issue" if prec == "fp64" else "fp32 issue / L1"}
+                   "peak_note": note, "flops_per_launch": fl, "frac": fl / per_launch_s / 1e12 / pk,
+                   "binding": {"fp64": "fp64 issue", "fp32": "fp32 issue / L1", "df": "fp32 issue"}[prec]}
         total_ms = sum(v["ms"] for v in kern.values())
         for k in kern:
             kern[k]["share"] = kern[k]["ms"] / total_ms

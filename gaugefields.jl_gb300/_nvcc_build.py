@@ -41,7 +41,9 @@ def up_to_date():
 
 
 def build(force=False, verbose=False, extra_flags=()):
-    """Compile every CUDA source for sm_103a and link libgfgb300.so."""
+    """Compile every CUDA source for sm_103a and link libgfgb300.so.
+    GF_NVCC_FLAGS (environment) adds tuning defines, e.g. -DGF_FP32_MINB=4."""
+    extra_flags = list(extra_flags) + os.environ.get("GF_NVCC_FLAGS", "").split()
     if not force and up_to_date():
         return LIB
     os.makedirs(BUILD, exist_ok=True)

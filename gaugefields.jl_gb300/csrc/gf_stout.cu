@@ -22,6 +22,14 @@
 #include "stencil.cuh"
 #include <type_traits>
 
+// Minimum resident blocks per SM requested for the fp32 stencil kernels
+// (register budget 65536 / (128 threads * GF_FP32_MINB)); fp64 variants keep
+// the full register file.
+#ifndef GF_FP32_MINB
+#define GF_FP32_MINB 3
+#endif
+#define GF_MINB(R) (sizeof(R) == 4 ? GF_FP32_MINB : 1)
+
 namespace gf {
 
 template <typename R>
@@ -76,11 +84,11 @@ __device__ __forceinline__ mat3<R> times_i(R r, const mat3<R>& a) {
 // forward level
 // --------------------------------------------------------------------------
 template <typename R>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, GF_MINB(R))
     k_stout_fwd(typename Prec<R>::Src U, typename Prec<R>::LinkElem* __restrict__ Uout,
                 typename Prec<R>::MatElem* __restrict__ Cout, Geom g, R rho) {
-  int s, mu;
-  link_of_block(s, mu);
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  int mu = blockIdx.y;
   if (s >= g.vol) return;
   const int V = g.vol;
   Site st = site_of(g, s);
@@ -98,12 +106,12 @@ __global__ void __launch_bounds__(128)
 // backward, local part
 // --------------------------------------------------------------------------
 template <typename R, bool TOP>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, GF_MINB(R))
     k_bwd_local(typename Prec<R>::Src U, typename Prec<R>::Src Utop, const typename Prec<R>::MatElem* __restrict__ Dbar,
                 const typename Prec<R>::MatElem* __restrict__ Cst, typename Prec<R>::MatElem* __restrict__ Zout,
                 typename Prec<R>::MatElem* __restrict__ Dpout, Geom g, R rho, R halfbeta) {
-  int s, mu;
-  link_of_block(s, mu);
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  int mu = blockIdx.y;
   if (s >= g.vol) return;
   const int V = g.vol;
   Site st = site_of(g, s);
@@ -212,12 +220,12 @@ __device__ __forceinline__ mat3<R> gather_all(const typename Prec<R>::Src& U,
 }
 
 template <typename R, bool FORCE>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, GF_MINB(R))
     k_bwd_gather(typename Prec<R>::Src U, const typename Prec<R>::MatElem* __restrict__ Z,
                  const typename Prec<R>::MatElem* __restrict__ Dp, typename Prec<R>::MatElem* __restrict__ Dout,
                  double* __restrict__ P, Geom g, R rho, double coef) {
-  int s, nu;
-  link_of_block(s, nu);
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  int nu = blockIdx.y;
   if (s >= g.vol) return;
   const int V = g.vol;
   Site st = site_of(g, s);
@@ -255,7 +263,7 @@ static typename Prec<R>::Src src_of(const gf_field* f) {
 
 template <typename R>
 static void forward_impl(gf_ctx* ctx, gf_stout* st) {
-  dim3 grid(4 * blocks_for(ctx->geom.vol, 128));
+  dim3 grid(blocks_for(ctx->geom.vol, 128), 4);
   for (int l = 0; l < st->nlev; ++l) {
     ProfScope prof(ctx, std::is_same<R, float>::value ? GF_K_STOUT_FWD
                         : (std::is_same<R, double>::value ? GF_K_STOUT_FWD64 : GF_K_STOUT_FWD_DF));
@@ -297,7 +305,7 @@ const gf_field* stout_top(const gf_stout* st) { return st->lev_in[st->nlev]; }
 template <typename R>
 static void backward_impl(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, double beta, gf_field* dSdU,
                           gf_field* P, double eps) {
-  dim3 grid(4 * blocks_for(ctx->geom.vol, 128));
+  dim3 grid(blocks_for(ctx->geom.vol, 128), 4);
   typedef typename Prec<R>::MatElem ME;
   const ME* dbar = dSdUbar ? (const ME*)dSdUbar->ptr : nullptr;
   int cur = 0;

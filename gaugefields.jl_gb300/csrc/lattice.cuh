@@ -75,16 +75,6 @@ GF_HD int nbr2(const Geom& g, const Site& st, int d0, int d1) {
   return eo_of_lex(g, lex, st.par);
 }
 
-// Stencil kernels run one thread per link on a 1-D grid of 4 * ceil(V/bs)
-// blocks; block b handles direction b % 4 of the sites of block b / 4, so the
-// four directions of the same sites run back to back and their shared
-// neighbour links are served from L2 instead of being re-read from HBM once
-// per direction.
-__device__ __forceinline__ void link_of_block(int& s, int& mu) {
-  mu = blockIdx.x & 3;
-  s = (blockIdx.x >> 2) * blockDim.x + threadIdx.x;
-}
-
 // ---------------------------------------------------------------------------
 // Field accessors. `V` is the site count, `s` the even/odd site index.
 // ---------------------------------------------------------------------------
