@@ -488,6 +488,81 @@ def run_wilson_mode(args):
     return 0
 
 
+def run_scale_mode(args):
+    """Memory-bound scale-up: `--lattice` (64) SU(3), 3-level stout rho = 0.1,
+    beta = 6.2, tau = 1, 30 QPQ steps, mixed precision, with the adjoint
+    storing each level's C (store) or recomputing it (recompute); peak device
+    memory of each, trajectories/s, one fp64 trajectory for the Delta H error,
+    then the RK3 flow eps = 0.01 to t = 3 recording E(t)."""
+    import numpy as np
+    import torch
+    import __graft_entry__ as entry
+    pkg = entry.build()
+    L = args.lattice
+    rho = (0.1, 0.1, 0.1)
+    free0, total = torch.cuda.mem_get_info()
+
+    def setup(prec, recompute):
+        U = pkg.gauge_configuration((L,) * 4, start="hot", seed=SEED)
+        P = pkg.gauge_momenta(U)
+        action = pkg.GaugeAction(U)
+        pkg.push_(action, 3.1, "plaquette")
+        net = pkg.CovNeuralnet(U)
+        for r in rho:
+            pkg.push_(net, pkg.STOUT_Layer("plaquette", r))
+        drv = pkg.md_driver(U, action, steps=30, trajectory_length=1.0, smearing=net, precision=prec,
+                            recompute=recompute)
+        return U, P, drv
+
+    out = {"mode": "scale", "lattice": [L] * 4, "workload": "%d^4, 3-level stout rho=0.1, beta=6.2, tau=1, "
+           "30 QPQ steps, mixed precision" % L}
+    U0 = None
+    for recompute in (False, True):
+        U, P, drv = setup("mixed", recompute)
+        if U0 is None:
+            U0 = U.to_host()
+        pkg.gaussian_momenta_(P, seed=SEED, sweep=0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = pkg.md_trajectory_(U, P, drv)
+        torch.cuda.synchronize()
+        first = time.perf_counter() - t0
+        used = total - torch.cuda.mem_get_info()[0] - (total - free0)
+        secs = []
+        for k in range(args.steps):
+            U.from_host(U0)
+            pkg.gaussian_momenta_(P, seed=SEED, sweep=k + 1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            pkg.md_trajectory_(U, P, drv)
+            torch.cuda.synchronize()
+            secs.append(time.perf_counter() - t0)
+        key = "recompute" if recompute else "store"
+        out[key] = {"device_GB": used / 1e9, "traj_per_s": 1.0 / min(secs), "dH_first": r.delta_hamiltonian,
+                    "first_trajectory_s": first}
+        del U, P, drv
+        torch.cuda.synchronize()
+    # Delta H of the first trajectory in the plain fp64 form
+    U, P, drv = setup("fp64", True)
+    U.from_host(U0)
+    pkg.gaussian_momenta_(P, seed=SEED, sweep=0)
+    t0 = time.perf_counter()
+    r64 = pkg.md_trajectory_(U, P, drv)
+    out["fp64"] = {"dH_first": r64.delta_hamiltonian, "trajectory_s": time.perf_counter() - t0}
+    out["abs_dH_diff"] = abs(out["store"]["dH_first"] - r64.delta_hamiltonian)
+    # RK3 Wilson flow to t = 3 on the configuration after that trajectory
+    g = pkg.Gradientflow(U, Nflow=1, eps=0.01)
+    E = []
+    t0 = time.perf_counter()
+    for k in range(300):
+        pkg.flow_(U, g)
+        if (k + 1) % 25 == 0:
+            E.append([round(0.01 * (k + 1), 2), 36.0 * (1.0 - pkg.measure_plaquette(U))])
+    out["flow"] = {"steps": 300, "seconds": time.perf_counter() - t0, "E_t": E}
+    print(json.dumps(out))
+    return 0
+
+
 def run_kernel_mode(args):
     """Small single-family cases for profiler captures: `force` repeats the
     mixed stout force (gf_stout_mom_update), `link` the fp64 link update."""
@@ -522,7 +597,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--therm", type=int, default=10, help="thermalisation trajectories before the Delta H check")
-    ap.add_argument("--mode", default="hmc", choices=["hmc", "force", "link", "precision", "wilson"],
+    ap.add_argument("--mode", default="hmc", choices=["hmc", "force", "link", "precision", "wilson", "scale"],
                     help="hmc: the benchmark; force/link: one kernel family, for profiler captures; "
                          "precision: mixed vs fp64 Delta H study from one thermalised configuration")
     args = ap.parse_args()
@@ -532,6 +607,8 @@ def main():
         return run_precision_mode(args)
     if args.mode == "wilson":
         return run_wilson_mode(args)
+    if args.mode == "scale":
+        return run_scale_mode(args)
     if args.mode != "hmc":
         return run_kernel_mode(args)
 

@@ -44,6 +44,7 @@ class MDParams(ctypes.Structure):
         ("nstout", ctypes.c_int),
         ("rho", ctypes.c_double * GF_MAX_STOUT),
         ("reunitarize", ctypes.c_int),
+        ("stout_recompute", ctypes.c_int),
     ]
 
 

@@ -338,7 +338,8 @@ class PQP:
 
 
 class MDDriver:
-    def __init__(self, action, integrator, trajectory_length, steps, smearing, precision, reunitarize):
+    def __init__(self, action, integrator, trajectory_length, steps, smearing, precision, reunitarize,
+                 recompute=False):
         self.action = action
         self.integrator = integrator
         self.trajectory_length = trajectory_length
@@ -346,6 +347,7 @@ class MDDriver:
         self.smearing = smearing
         self.precision = precision
         self.reunitarize = reunitarize
+        self.recompute = recompute
         self._stout = None
 
     def params(self):
@@ -360,17 +362,20 @@ class MDDriver:
         for i, r in enumerate(rho):
             p.rho[i] = r
         p.reunitarize = 1 if self.reunitarize else 0
+        p.stout_recompute = 1 if self.recompute else 0
         return p
 
 
 def md_driver(U, action, steps, trajectory_length=1.0, integrator=None, smearing=None, precision="fp64",
-              reunitarize=True):
+              reunitarize=True, recompute=False):
     """md_driver(U, action; steps, trajectory_length, integrator) (molecular_dynamics.jl:440-483).
 
     smearing: a CovNeuralnet of stout layers; the action is then evaluated on
     the smeared links and the force is back-propagated to the thin links.
     precision: "fp64" (plain form) or "mixed" (fp32 force and stout on 12-real
-    links; fp64 Hamiltonian, Delta H, link updates and re-unitarisation)."""
+    links; fp64-class Hamiltonian, Delta H, link updates and re-unitarisation).
+    recompute: the stout adjoint rebuilds each level's staple sum C instead of
+    keeping it from the forward pass (less device memory)."""
     integrator = integrator if integrator is not None else QPQ()
     if len(U) != 4:
         raise ValueError("the gauge configuration has length %d; expected 4" % len(U))
@@ -386,7 +391,8 @@ def md_driver(U, action, steps, trajectory_length=1.0, integrator=None, smearing
         raise ValueError("md_step! is not implemented for %s" % type(integrator).__name__)
     if not isinstance(action, GaugeAction) or not action.terms:
         raise ValueError("md_action_workspace is not implemented for %s" % type(action).__name__)
-    return MDDriver(action, integrator, float(trajectory_length), int(steps), smearing, precision, reunitarize)
+    return MDDriver(action, integrator, float(trajectory_length), int(steps), smearing, precision, reunitarize,
+                    recompute)
 
 
 def md_step_size(driver):
@@ -431,7 +437,7 @@ def update_gaugefields_(U, P, step_size, driver):
 
 def _stout_for(driver, U):
     if driver._stout is None:
-        driver._stout = _StoutStack(U.ctx, driver.smearing.rhos(), driver.precision)
+        driver._stout = _StoutStack(U.ctx, driver.smearing.rhos(), driver.precision, store=not driver.recompute)
     return driver._stout
 
 

@@ -448,22 +448,28 @@ static void check_md(const gf_md_params* p) {
 static gf_stout* ctx_stout(gf_ctx* ctx, const gf_md_params* p, int precision) {
   gf_stout** slot = precision == GF_FP64 ? &ctx->w_stout64
                     : (precision == GF_MIXED ? &ctx->w_stout32 : &ctx->w_stoutdf);
-  bool same = *slot && (*slot)->nlev == p->nstout;
+  int store = (precision == GF_PREC_DF) ? 0 : (p->stout_recompute ? 0 : 1);
+  bool same = *slot && (*slot)->nlev == p->nstout && (*slot)->store == store;
   if (same)
     for (int l = 0; l < p->nstout; ++l) same = same && (*slot)->rho[l] == p->rho[l];
   if (!same) {
     if (*slot) gf_stout_destroy(*slot);
     *slot = nullptr;
-    *slot = stout_new(ctx, p->nstout, p->rho, precision, 1);
+    *slot = stout_new(ctx, p->nstout, p->rho, precision, store);
   }
   return *slot;
 }
 
-// The potential on the (smeared) fp64 links. The plain form computes it in
-// fp64; the mixed form in double-float arithmetic (~1e-14 per operation) on
-// the fp32 pipes, with fp64 storage and fp64 global sums.
+// The potential on the (smeared) fp64 links, in fp64. With
+// GF_DF_HAMILTONIAN the mixed form evaluates it in double-float arithmetic
+// (~1e-14 per operation) on the fp32 pipes instead, with fp64 storage and
+// fp64 global sums; on GB300 the fp64 form of this stencil is currently the
+// faster one.
+#ifndef GF_DF_HAMILTONIAN
+#define GF_DF_HAMILTONIAN 0
+#endif
 static double potential(gf_ctx* ctx, const gf_field* U, const gf_md_params* p) {
-  bool df = p->precision == GF_MIXED;
+  bool df = GF_DF_HAMILTONIAN && p->precision == GF_MIXED;
   if (p->nstout == 0) return -(p->beta / 3.0) * plaquette_sum(ctx, U, df);
   gf_stout* st = ctx_stout(ctx, p, df ? GF_PREC_DF : GF_FP64);
   stout_forward(ctx, st, U, nullptr);

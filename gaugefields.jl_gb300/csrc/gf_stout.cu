@@ -26,7 +26,7 @@
 // (register budget 65536 / (128 threads * GF_FP32_MINB)); fp64 variants keep
 // the full register file.
 #ifndef GF_FP32_MINB
-#define GF_FP32_MINB 3
+#define GF_FP32_MINB 4
 #endif
 #define GF_MINB(R) (sizeof(R) == 4 ? GF_FP32_MINB : 1)
 
@@ -87,8 +87,8 @@ template <typename R>
 __global__ void __launch_bounds__(128, GF_MINB(R))
     k_stout_fwd(typename Prec<R>::Src U, typename Prec<R>::LinkElem* __restrict__ Uout,
                 typename Prec<R>::MatElem* __restrict__ Cout, Geom g, R rho) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  int mu = blockIdx.y;
+  int s, mu;
+  link_of_thread(s, mu);
   if (s >= g.vol) return;
   const int V = g.vol;
   Site st = site_of(g, s);
@@ -110,8 +110,8 @@ __global__ void __launch_bounds__(128, GF_MINB(R))
     k_bwd_local(typename Prec<R>::Src U, typename Prec<R>::Src Utop, const typename Prec<R>::MatElem* __restrict__ Dbar,
                 const typename Prec<R>::MatElem* __restrict__ Cst, typename Prec<R>::MatElem* __restrict__ Zout,
                 typename Prec<R>::MatElem* __restrict__ Dpout, Geom g, R rho, R halfbeta) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  int mu = blockIdx.y;
+  int s, mu;
+  link_of_thread(s, mu);
   if (s >= g.vol) return;
   const int V = g.vol;
   Site st = site_of(g, s);
@@ -172,15 +172,15 @@ __global__ void __launch_bounds__(128, GF_MINB(R))
 //  (a) U_K(x+nu) U_nu(x+K)^dag Z_K(x)          (b) U_K(x-K+nu)^dag U_nu(x-K)^dag Z_K(x-K)^dag
 //  (c) Z_K(x+nu)^dag U_nu(x+K)^dag U_K(x)^dag  (d) Z_K(x+nu-K) U_nu(x-K)^dag U_K(x-K)
 //  (e) U_K(x-K+nu)^dag Z_nu(x-K) U_K(x-K)      (f) U_K(x+nu) Z_nu(x+K) U_K(x)^dag
-template <typename R, int NU, int K>
+template <typename R>
 __device__ __forceinline__ void gather_axis(mat3<R>& acc, const typename Prec<R>::Src& U,
                                             const typename Prec<R>::MatElem* __restrict__ Z, const Geom& g,
-                                            const Site& st, int s) {
+                                            const Site& st, int s, int NU, int K) {
   const int V = g.vol;
-  const int xpn = nbr<NU>(g, st, +1);
-  const int xpk = nbr<K>(g, st, +1);
-  const int xmk = nbr<K>(g, st, -1);
-  const int xmk_pn = nbr2<K, NU>(g, st, -1, +1);
+  const int xpn = nbr_rt(g, st, NU, +1);
+  const int xpk = nbr_rt(g, st, K, +1);
+  const int xmk = nbr_rt(g, st, K, -1);
+  const int xmk_pn = nbr2_rt(g, st, K, -1, NU, +1);
   {
     mat3<R> a1 = U(K, xpn, V);   // U_K(x+nu)
     mat3<R> a2 = U(NU, xpk, V);  // U_nu(x+K)
@@ -207,35 +207,19 @@ __device__ __forceinline__ void gather_axis(mat3<R>& acc, const typename Prec<R>
   }
 }
 
-template <typename R, int NU>
-__device__ __forceinline__ mat3<R> gather_all(const typename Prec<R>::Src& U,
-                                              const typename Prec<R>::MatElem* __restrict__ Z, const Geom& g,
-                                              const Site& st, int s) {
-  mat3<R> acc = zero3<R>();
-  if constexpr (NU != 0) gather_axis<R, NU, 0>(acc, U, Z, g, st, s);
-  if constexpr (NU != 1) gather_axis<R, NU, 1>(acc, U, Z, g, st, s);
-  if constexpr (NU != 2) gather_axis<R, NU, 2>(acc, U, Z, g, st, s);
-  if constexpr (NU != 3) gather_axis<R, NU, 3>(acc, U, Z, g, st, s);
-  return acc;
-}
-
 template <typename R, bool FORCE>
 __global__ void __launch_bounds__(128, GF_MINB(R))
     k_bwd_gather(typename Prec<R>::Src U, const typename Prec<R>::MatElem* __restrict__ Z,
                  const typename Prec<R>::MatElem* __restrict__ Dp, typename Prec<R>::MatElem* __restrict__ Dout,
                  double* __restrict__ P, Geom g, R rho, double coef) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  int nu = blockIdx.y;
+  int s, nu;
+  link_of_thread(s, nu);
   if (s >= g.vol) return;
   const int V = g.vol;
   Site st = site_of(g, s);
-  mat3<R> acc;
-  switch (nu) {
-    case 0: acc = gather_all<R, 0>(U, Z, g, st, s); break;
-    case 1: acc = gather_all<R, 1>(U, Z, g, st, s); break;
-    case 2: acc = gather_all<R, 2>(U, Z, g, st, s); break;
-    default: acc = gather_all<R, 3>(U, Z, g, st, s); break;
-  }
+  mat3<R> acc = zero3<R>();
+#pragma unroll 1
+  for (int k = 1; k < 4; ++k) gather_axis<R>(acc, U, Z, g, st, s, nu, (nu + k) & 3);
   mat3<R> d = LinkFull<R>::load(Dp, nu, s, V);
   axpy_to(d, rho, acc);
   if (FORCE) {
@@ -263,7 +247,7 @@ static typename Prec<R>::Src src_of(const gf_field* f) {
 
 template <typename R>
 static void forward_impl(gf_ctx* ctx, gf_stout* st) {
-  dim3 grid(blocks_for(ctx->geom.vol, 128), 4);
+  dim3 grid = stencil_grid(ctx->geom.vol, 128);
   for (int l = 0; l < st->nlev; ++l) {
     ProfScope prof(ctx, std::is_same<R, float>::value ? GF_K_STOUT_FWD
                         : (std::is_same<R, double>::value ? GF_K_STOUT_FWD64 : GF_K_STOUT_FWD_DF));
@@ -305,7 +289,7 @@ const gf_field* stout_top(const gf_stout* st) { return st->lev_in[st->nlev]; }
 template <typename R>
 static void backward_impl(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, double beta, gf_field* dSdU,
                           gf_field* P, double eps) {
-  dim3 grid(blocks_for(ctx->geom.vol, 128), 4);
+  dim3 grid = stencil_grid(ctx->geom.vol, 128);
   typedef typename Prec<R>::MatElem ME;
   const ME* dbar = dSdUbar ? (const ME*)dSdUbar->ptr : nullptr;
   int cur = 0;

@@ -80,8 +80,8 @@ void staple_up(gf_ctx* ctx, const gf_field* U, int mu, gf_field* Vout) {
 //  * add_force! flow:  coef = factor
 template <typename R, class SRC>
 __global__ void __launch_bounds__(128) k_force_ta(SRC U, double* __restrict__ P, Geom g, double coef, double keep) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  int mu = blockIdx.y;
+  int s, mu;
+  link_of_thread(s, mu);
   if (s >= g.vol) return;
   Site st = site_of(g, s);
   const int V = g.vol;
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(128) k_force_ta(SRC U, double* __restrict__ P,
 
 void wilson_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double coef, double keep) {
   if (P->kind != GF_MOM64) throw gf_error(GF_EINVAL, "force: output must be MOM64");
-  dim3 grid(blocks_for(ctx->geom.vol, 128), 4);
+  dim3 grid = stencil_grid(ctx->geom.vol, 128);
   ProfScope prof(ctx, GF_K_FORCE);
   if (U->kind == GF_LINK64) {
     Src64 src{(const double2*)U->ptr};

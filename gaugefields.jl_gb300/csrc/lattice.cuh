@@ -75,6 +75,54 @@ GF_HD int nbr2(const Geom& g, const Site& st, int d0, int d1) {
   return eo_of_lex(g, lex, st.par);
 }
 
+// Link index of a stencil thread. With GF_INTERLEAVE the grid is 1-D with
+// 4 * ceil(V/bs) blocks and block b handles direction b % 4 of the sites of
+// block b / 4 (the four directions of the same sites run back to back, so
+// their shared neighbours stay in L2); otherwise blockIdx.y is the direction.
+#ifndef GF_INTERLEAVE
+#define GF_INTERLEAVE 0
+#endif
+__device__ __forceinline__ void link_of_thread(int& s, int& mu) {
+#if GF_INTERLEAVE
+  mu = blockIdx.x & 3;
+  s = (blockIdx.x >> 2) * blockDim.x + threadIdx.x;
+#else
+  mu = blockIdx.y;
+  s = blockIdx.x * blockDim.x + threadIdx.x;
+#endif
+}
+inline dim3 stencil_grid(int vol, int bs) {
+#if GF_INTERLEAVE
+  return dim3(4 * ((vol + bs - 1) / bs));
+#else
+  return dim3((vol + bs - 1) / bs, 4);
+#endif
+}
+
+// Runtime-axis forms of the same steps. The stencil kernels loop over the
+// other axes at run time (one loop body instead of one unrolled copy per axis
+// pair), which keeps their code within the instruction cache.
+GF_HD int coord(const Site& st, int mu) {
+  return mu == 0 ? st.x[0] : (mu == 1 ? st.x[1] : (mu == 2 ? st.x[2] : st.x[3]));
+}
+GF_HD int step_lex_rt(const Geom& g, int lex, int c, int mu, int d) {
+  const int L = g.L[mu], str = g.stride[mu];
+  const int n = c + d;
+  if (n < 0) return lex + (L - 1) * str;
+  if (n >= L) return lex - (L - 1) * str;
+  return lex + d * str;
+}
+// even/odd index of x + d e_mu
+GF_HD int nbr_rt(const Geom& g, const Site& st, int mu, int d) {
+  return eo_of_lex(g, step_lex_rt(g, st.lex, coord(st, mu), mu, d), st.par ^ 1);
+}
+// even/odd index of x + d0 e_mu + d1 e_nu  (mu != nu)
+GF_HD int nbr2_rt(const Geom& g, const Site& st, int mu, int d0, int nu, int d1) {
+  int lex = step_lex_rt(g, st.lex, coord(st, mu), mu, d0);
+  lex = step_lex_rt(g, lex, coord(st, nu), nu, d1);
+  return eo_of_lex(g, lex, st.par);
+}
+
 // ---------------------------------------------------------------------------
 // Field accessors. `V` is the site count, `s` the even/odd site index.
 // ---------------------------------------------------------------------------

@@ -64,39 +64,29 @@ __device__ __forceinline__ void mac_aa(mat3<R>& acc, const mat3<R>& a, const mat
     }
 }
 
-template <typename R, class SRC, int MU, int NU>
-__device__ __forceinline__ void add_staple_pair(mat3<R>& acc, const SRC& U, const Geom& g, const Site& st, int s) {
+template <typename R, class SRC>
+__device__ __forceinline__ void add_staple_pair(mat3<R>& acc, const SRC& U, const Geom& g, const Site& st, int s,
+                                                int mu, int nu) {
   const int V = g.vol;
-  const int xpm = nbr<MU>(g, st, +1);
-  const int xpn = nbr<NU>(g, st, +1);
-  const int xmn = nbr<NU>(g, st, -1);
-  const int xpm_mn = nbr2<MU, NU>(g, st, +1, -1);
+  const int xpm = nbr_rt(g, st, mu, +1);
+  const int xpn = nbr_rt(g, st, nu, +1);
+  const int xmn = nbr_rt(g, st, nu, -1);
+  const int xpm_mn = nbr2_rt(g, st, mu, +1, nu, -1);
   // up: U_nu(x+mu) U_mu(x+nu)^dag U_nu(x)^dag
-  mat3<R> t = mul_na(U(NU, xpm, V), U(MU, xpn, V));
-  mac_na(acc, t, U(NU, s, V));
+  mat3<R> t = mul_na(U(nu, xpm, V), U(mu, xpn, V));
+  mac_na(acc, t, U(nu, s, V));
   // down: U_nu(x+mu-nu)^dag U_mu(x-nu)^dag U_nu(x-nu)
-  t = mul_aa(U(NU, xpm_mn, V), U(MU, xmn, V));
-  mac_nn(acc, t, U(NU, xmn, V));
+  t = mul_aa(U(nu, xpm_mn, V), U(mu, xmn, V));
+  mac_nn(acc, t, U(nu, xmn, V));
 }
 
-template <typename R, class SRC, int MU>
-__device__ __forceinline__ mat3<R> staple_sum_mu(const SRC& U, const Geom& g, const Site& st, int s) {
-  mat3<R> acc = zero3<R>();
-  if constexpr (MU != 0) add_staple_pair<R, SRC, MU, 0>(acc, U, g, st, s);
-  if constexpr (MU != 1) add_staple_pair<R, SRC, MU, 1>(acc, U, g, st, s);
-  if constexpr (MU != 2) add_staple_pair<R, SRC, MU, 2>(acc, U, g, st, s);
-  if constexpr (MU != 3) add_staple_pair<R, SRC, MU, 3>(acc, U, g, st, s);
-  return acc;
-}
-
+// S_mu(x); the three other axes nu = mu+1, mu+2, mu+3 (mod 4) in a run-time loop
 template <typename R, class SRC>
 __device__ __forceinline__ mat3<R> staple_sum(int mu, const SRC& U, const Geom& g, const Site& st, int s) {
-  switch (mu) {
-    case 0: return staple_sum_mu<R, SRC, 0>(U, g, st, s);
-    case 1: return staple_sum_mu<R, SRC, 1>(U, g, st, s);
-    case 2: return staple_sum_mu<R, SRC, 2>(U, g, st, s);
-    default: return staple_sum_mu<R, SRC, 3>(U, g, st, s);
-  }
+  mat3<R> acc = zero3<R>();
+#pragma unroll 1
+  for (int k = 1; k < 4; ++k) add_staple_pair<R>(acc, U, g, st, s, mu, (mu + k) & 3);
+  return acc;
 }
 
 // Sum over mu<nu of Re tr P_munu(x) at one site.

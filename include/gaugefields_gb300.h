@@ -69,6 +69,9 @@ typedef struct gf_md_params {
   int nstout;            /* 0 .. GF_MAX_STOUT smearing levels */
   double rho[GF_MAX_STOUT];
   int reunitarize;       /* re-unitarise links after every link update */
+  int stout_recompute;   /* 1: the adjoint recomputes each level's C_mu from the
+                            stored level input instead of keeping it from the
+                            forward pass (less memory, more flops) */
 } gf_md_params;
 
 /* ---- context ------------------------------------------------------------ */

@@ -247,6 +247,23 @@ def test_stout_force(pkg, oracle, L):
     assert frob_mom(P.to_host(), ref) < 1e-11
 
 
+def test_stout_recompute_matches_store(pkg):
+    """Recomputing each level's C in the adjoint gives the stored-C force."""
+    out = []
+    for recompute in (False, True):
+        U = pkg.gauge_configuration(L4, start="hot", seed=13)
+        P = pkg.gauge_momenta(U)
+        action = pkg.GaugeAction(U)
+        pkg.push_(action, 3.0, "plaquette")
+        net = pkg.stout_smearing(U, rho=0.1)
+        pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.12))
+        pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.08))
+        drv = pkg.md_driver(U, action, steps=1, smearing=net, recompute=recompute)
+        pkg.update_momenta_(P, U, 1.0, drv)
+        out.append(P.to_host())
+    assert frob_mom(out[0], out[1]) < 1e-14
+
+
 def test_stout_force_finite_differences(pkg):
     """config 3(a): central differences, h = 1e-5, along 16 random su(3)
     directions at random links of a 4^4 lattice, of the GPU potential."""
