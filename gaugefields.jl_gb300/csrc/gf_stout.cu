@@ -22,13 +22,7 @@
 #include "stencil.cuh"
 #include <type_traits>
 
-// Minimum resident blocks per SM requested for the fp32 stencil kernels
-// (register budget 65536 / (128 threads * GF_FP32_MINB)); fp64 variants keep
-// the full register file.
-#ifndef GF_FP32_MINB
-#define GF_FP32_MINB 4
-#endif
-#define GF_MINB(R) (sizeof(R) == 4 ? GF_FP32_MINB : 1)
+
 
 namespace gf {
 

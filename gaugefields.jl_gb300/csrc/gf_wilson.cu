@@ -11,7 +11,7 @@ typedef LinkSrc<float, true> Src32;
 // Per-site plaquette sum, one partial per block (calculate_Plaquette,
 // src/AbstractGaugefields.jl:2684-2699, evaluated plaquette by plaquette).
 template <typename R, class SRC>
-__global__ void __launch_bounds__(128) k_plaquette(SRC U, Geom g, double* __restrict__ part) {
+__global__ void __launch_bounds__(128, GF_MINB(R)) k_plaquette(SRC U, Geom g, double* __restrict__ part) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   double v = 0.0;
   if (s < g.vol) {
@@ -79,7 +79,7 @@ void staple_up(gf_ctx* ctx, const gf_field* U, int mu, gf_field* Vout) {
 //  * update_momenta!:  coef = eps * (-(1/3) * beta/2), keep = 1
 //  * add_force! flow:  coef = factor
 template <typename R, class SRC>
-__global__ void __launch_bounds__(128) k_force_ta(SRC U, double* __restrict__ P, Geom g, double coef, double keep) {
+__global__ void __launch_bounds__(128, GF_MINB(R)) k_force_ta(SRC U, double* __restrict__ P, Geom g, double coef, double keep) {
   int s, mu;
   link_of_thread(s, mu);
   if (s >= g.vol) return;

@@ -75,12 +75,36 @@ GF_HD int nbr2(const Geom& g, const Site& st, int d0, int d1) {
   return eo_of_lex(g, lex, st.par);
 }
 
+// Minimum resident blocks per SM requested for the stencil kernels (register
+// budget 65536 / (128 threads * min blocks)): fp32 and double-float kernels are
+// latency-bound and gain from occupancy; fp64 kernels are fp64-issue-bound and
+// keep the full register file.
+#ifndef GF_FP32_MINB
+#define GF_FP32_MINB 4
+#endif
+#ifndef GF_DF_MINB
+#define GF_DF_MINB 2
+#endif
+template <typename R>
+struct minblocks {
+  static constexpr int value = 1;
+};
+template <>
+struct minblocks<float> {
+  static constexpr int value = GF_FP32_MINB;
+};
+template <>
+struct minblocks<dfl> {
+  static constexpr int value = GF_DF_MINB;
+};
+#define GF_MINB(R) (minblocks<R>::value)
+
 // Link index of a stencil thread. With GF_INTERLEAVE the grid is 1-D with
 // 4 * ceil(V/bs) blocks and block b handles direction b % 4 of the sites of
 // block b / 4 (the four directions of the same sites run back to back, so
 // their shared neighbours stay in L2); otherwise blockIdx.y is the direction.
 #ifndef GF_INTERLEAVE
-#define GF_INTERLEAVE 0
+#define GF_INTERLEAVE 1
 #endif
 __device__ __forceinline__ void link_of_thread(int& s, int& mu) {
 #if GF_INTERLEAVE

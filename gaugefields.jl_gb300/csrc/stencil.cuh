@@ -64,6 +64,20 @@ __device__ __forceinline__ void mac_aa(mat3<R>& acc, const mat3<R>& a, const mat
     }
 }
 
+// double-float accumulating products as compensated dot products
+__device__ __forceinline__ void mac_nn(mat3<dfl>& acc, const mat3<dfl>& a, const mat3<dfl>& b) {
+  acc = df_matmul<false, false, true>(a, b, &acc);
+}
+__device__ __forceinline__ void mac_na(mat3<dfl>& acc, const mat3<dfl>& a, const mat3<dfl>& b) {
+  acc = df_matmul<false, true, true>(a, b, &acc);
+}
+__device__ __forceinline__ void mac_an(mat3<dfl>& acc, const mat3<dfl>& a, const mat3<dfl>& b) {
+  acc = df_matmul<true, false, true>(a, b, &acc);
+}
+__device__ __forceinline__ void mac_aa(mat3<dfl>& acc, const mat3<dfl>& a, const mat3<dfl>& b) {
+  acc = df_matmul<true, true, true>(a, b, &acc);
+}
+
 template <typename R, class SRC>
 __device__ __forceinline__ void add_staple_pair(mat3<R>& acc, const SRC& U, const Geom& g, const Site& st, int s,
                                                 int mu, int nu) {

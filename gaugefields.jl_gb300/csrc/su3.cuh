@@ -523,3 +523,75 @@ __device__ __forceinline__ mat3<R> expiq(const mat3<R>& q, mat3<R>* q2out = null
 }
 
 }  // namespace gf
+
+// ---------------------------------------------------------------------------
+// Double-float 3x3 products as compensated dot products (Ogita, Rump, Oishi,
+// "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005, Dot2 with
+// double-float inputs): the high parts are summed with TwoSum, the product
+// errors (FMA), the TwoSum errors and the cross terms hi*lo + lo*hi go into a
+// single fp32 correction. Error ~ u^2 * sum |terms|, about half the operations
+// of composing double-float multiplies and adds.
+// ---------------------------------------------------------------------------
+namespace gf {
+
+struct dacc {
+  float s, c;
+};
+
+GF_HD void dacc_add(dacc& a, float xh, float xl, float yh, float yl) {
+  float p = xh * yh;
+  float pe = fmaf(xh, yh, -p);
+  float t = a.s + p;
+  float z = t - a.s;
+  float e = (a.s - (t - z)) + (p - z);
+  a.s = t;
+  a.c += e + pe;
+  a.c = fmaf(xh, yl, a.c);
+  a.c = fmaf(xl, yh, a.c);
+}
+
+GF_HD dfl dacc_get(const dacc& a) { return df_two_sum(a.s, a.c); }
+
+// acc(i,j) (+)= sum_k op(a)_ik op(b)_kj with op = identity or dagger
+template <bool DA, bool DB, bool ACC>
+GF_HD mat3<dfl> df_matmul(const mat3<dfl>& a, const mat3<dfl>& b, const mat3<dfl>* c) {
+  mat3<dfl> r;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      dacc re, im;
+      if (ACC) {
+        re.s = c->e[i][j].re.hi; re.c = c->e[i][j].re.lo;
+        im.s = c->e[i][j].im.hi; im.c = c->e[i][j].im.lo;
+      } else {
+        re.s = re.c = im.s = im.c = 0.f;
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const cplx<dfl> x = DA ? conj(a.e[k][i]) : a.e[i][k];
+        const cplx<dfl> y = DB ? conj(b.e[j][k]) : b.e[k][j];
+        dacc_add(re, x.re.hi, x.re.lo, y.re.hi, y.re.lo);
+        dacc_add(re, -x.im.hi, -x.im.lo, y.im.hi, y.im.lo);
+        dacc_add(im, x.re.hi, x.re.lo, y.im.hi, y.im.lo);
+        dacc_add(im, x.im.hi, x.im.lo, y.re.hi, y.re.lo);
+      }
+      r.e[i][j] = mk(dacc_get(re), dacc_get(im));
+    }
+  return r;
+}
+
+__device__ __forceinline__ mat3<dfl> mul_nn(const mat3<dfl>& a, const mat3<dfl>& b) {
+  return df_matmul<false, false, false>(a, b, nullptr);
+}
+__device__ __forceinline__ mat3<dfl> mul_na(const mat3<dfl>& a, const mat3<dfl>& b) {
+  return df_matmul<false, true, false>(a, b, nullptr);
+}
+__device__ __forceinline__ mat3<dfl> mul_an(const mat3<dfl>& a, const mat3<dfl>& b) {
+  return df_matmul<true, false, false>(a, b, nullptr);
+}
+__device__ __forceinline__ mat3<dfl> mul_aa(const mat3<dfl>& a, const mat3<dfl>& b) {
+  return df_matmul<true, true, false>(a, b, nullptr);
+}
+
+}  // namespace gf
