@@ -83,7 +83,7 @@ GF_HD int nbr2(const Geom& g, const Site& st, int d0, int d1) {
 #define GF_FP32_MINB 4
 #endif
 #ifndef GF_DF_MINB
-#define GF_DF_MINB 2
+#define GF_DF_MINB 3
 #endif
 template <typename R>
 struct minblocks {
