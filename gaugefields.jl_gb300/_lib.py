@@ -18,7 +18,7 @@ GF_ESTATE = -5
 
 GF_LINK64, GF_LINK32, GF_MOM64, GF_MAT64, GF_MAT32 = 1, 2, 3, 4, 5
 GF_FP64, GF_MIXED = 0, 1
-GF_QPQ, GF_PQP = 0, 1
+GF_QPQ, GF_PQP, GF_OMELYAN = 0, 1, 2
 GF_MAX_STOUT = 4
 
 
@@ -45,6 +45,7 @@ class MDParams(ctypes.Structure):
         ("rho", ctypes.c_double * GF_MAX_STOUT),
         ("reunitarize", ctypes.c_int),
         ("stout_recompute", ctypes.c_int),
+        ("lam", ctypes.c_double),
     ]
 
 

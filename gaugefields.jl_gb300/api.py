@@ -23,7 +23,7 @@ from ._lib import MDParams, call
 __all__ = [
     "GB300Backend", "gauge_configuration", "measure_plaquette", "calculate_Plaquette", "construct_staple_",
     "gauge_momenta", "gaussian_momenta_", "gaussian_momenta", "GaugeAction", "push_", "evaluate_GaugeAction",
-    "QPQ", "PQP", "md_driver", "md_step_size", "md_hamiltonian", "md_potential", "md_force_",
+    "QPQ", "PQP", "OmelyanPQP", "md_driver", "md_step_size", "md_hamiltonian", "md_potential", "md_force_",
     "md_action_workspace", "update_gaugefields_", "update_momenta_", "md_step_", "md_trajectory_",
     "hmc_update_", "STOUT_Layer", "CovNeuralnet", "stout_smearing", "smear", "calc_smearedU", "back_prop",
     "Gradientflow", "gradient_flow", "flow_", "add_force_", "energy_density_plaquette", "substitute_U_",
@@ -337,6 +337,16 @@ class PQP:
     """Leapfrog with half momentum steps at both ends (molecular_dynamics.jl:604-609)."""
 
 
+class OmelyanPQP:
+    """Second-order minimum-norm integrator, the reference's custom-integrator
+    example (docs/src/hmc.md:250-270): P(l e) Q(e/2) P((1-2l) e) Q(e/2) P(l e)."""
+
+    def __init__(self, lam=0.1931833275037836):
+        if not math.isfinite(lam):
+            raise ValueError("lambda must be finite")
+        self.lam = float(lam)
+
+
 class MDDriver:
     def __init__(self, action, integrator, trajectory_length, steps, smearing, precision, reunitarize,
                  recompute=False):
@@ -355,7 +365,11 @@ class MDDriver:
         p.beta = self.action.beta
         p.tau = self.trajectory_length
         p.steps = self.steps
-        p.integrator = _lib.GF_PQP if isinstance(self.integrator, PQP) else _lib.GF_QPQ
+        if isinstance(self.integrator, OmelyanPQP):
+            p.integrator = _lib.GF_OMELYAN
+            p.lam = self.integrator.lam
+        else:
+            p.integrator = _lib.GF_PQP if isinstance(self.integrator, PQP) else _lib.GF_QPQ
         p.precision = _lib.GF_MIXED if self.precision == "mixed" else _lib.GF_FP64
         rho = self.smearing.rhos() if self.smearing is not None else []
         p.nstout = len(rho)
@@ -387,7 +401,7 @@ def md_driver(U, action, steps, trajectory_length=1.0, integrator=None, smearing
         raise ValueError("trajectory_length must not be zero")
     if precision not in ("fp64", "mixed"):
         raise ValueError("precision must be 'fp64' or 'mixed'")
-    if not (isinstance(integrator, (QPQ, PQP)) or callable(integrator)):
+    if not (isinstance(integrator, (QPQ, PQP, OmelyanPQP)) or callable(integrator)):
         raise ValueError("md_step! is not implemented for %s" % type(integrator).__name__)
     if not isinstance(action, GaugeAction) or not action.terms:
         raise ValueError("md_action_workspace is not implemented for %s" % type(action).__name__)
@@ -470,6 +484,13 @@ def md_step_(integrator, U, P, step_size, driver):
         update_momenta_(P, U, step_size / 2, driver)
         update_gaugefields_(U, P, step_size, driver)
         update_momenta_(P, U, step_size / 2, driver)
+    elif isinstance(integrator, OmelyanPQP):
+        lam = integrator.lam
+        update_momenta_(P, U, lam * step_size, driver)
+        update_gaugefields_(U, P, 0.5 * step_size, driver)
+        update_momenta_(P, U, (1 - 2 * lam) * step_size, driver)
+        update_gaugefields_(U, P, 0.5 * step_size, driver)
+        update_momenta_(P, U, lam * step_size, driver)
     elif isinstance(integrator, QPQ):
         update_gaugefields_(U, P, step_size / 2, driver)
         update_momenta_(P, U, step_size, driver)
@@ -486,7 +507,7 @@ MDResult = namedtuple("MDResult", ["initial_hamiltonian", "final_hamiltonian", "
 def md_trajectory_(U, P, driver, diagnostics=True):
     """md_trajectory!(U, P, driver) (molecular_dynamics.jl:712-730). The builtin
     QPQ/PQP run as one native call; custom integrators step from Python."""
-    if isinstance(driver.integrator, (QPQ, PQP)):
+    if isinstance(driver.integrator, (QPQ, PQP, OmelyanPQP)):
         p = driver.params()
         out = (ctypes.c_double * 3)()
         call("gf_md_trajectory", U.ctx.h, U.field.h, P.field.h, ctypes.byref(p), out, ctx=U.ctx.h)
@@ -507,7 +528,7 @@ HMCResult = namedtuple("HMCResult", ["initial_hamiltonian", "final_hamiltonian",
 def hmc_update_(U, P, driver, seed, sweep, unif):
     """Momentum refresh + md_trajectory! + Metropolis (docs/src/hmc.md:22-81);
     a rejected trajectory restores U."""
-    if not isinstance(driver.integrator, (QPQ, PQP)):
+    if not isinstance(driver.integrator, (QPQ, PQP, OmelyanPQP)):
         raise ValueError("hmc_update_ runs the builtin integrators natively")
     p = driver.params()
     out = (ctypes.c_double * 4)()

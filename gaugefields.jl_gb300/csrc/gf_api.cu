@@ -439,7 +439,9 @@ static void check_md(const gf_md_params* p) {
   need(std::isfinite(p->tau), "md: trajectory_length must be finite");
   need(p->tau != 0.0, "md: trajectory_length must not be zero");
   need(std::isfinite(p->beta), "md: beta must be finite");
-  need(p->integrator == GF_QPQ || p->integrator == GF_PQP, "md: integrator must be GF_QPQ or GF_PQP");
+  need(p->integrator == GF_QPQ || p->integrator == GF_PQP || p->integrator == GF_OMELYAN,
+       "md: integrator must be GF_QPQ, GF_PQP or GF_OMELYAN");
+  need(p->integrator != GF_OMELYAN || std::isfinite(p->lambda), "md: the Omelyan lambda must be finite");
   need(p->precision == GF_FP64 || p->precision == GF_MIXED, "md: precision must be GF_FP64 or GF_MIXED");
   need(p->nstout >= 0 && p->nstout <= GF_MAX_STOUT, "md: nstout must be 0..GF_MAX_STOUT");
   for (int l = 0; l < p->nstout; ++l) need(std::isfinite(p->rho[l]), "md: rho must be finite");
@@ -549,11 +551,22 @@ static MDResult md_run(gf_ctx* ctx, gf_field* U, gf_field* P, const gf_md_params
       mom_update(ctx, P, U, U32, eps, p);
       link_update(ctx, U, P, (n == p->steps - 1) ? 0.5 * eps : eps, p->reunitarize, U32, df);
     }
-  } else {
+  } else if (p->integrator == GF_PQP) {
     mom_update(ctx, P, U, U32, 0.5 * eps, p);
     for (int n = 0; n < p->steps; ++n) {
       link_update(ctx, U, P, eps, p->reunitarize, U32, df);
       mom_update(ctx, P, U, U32, (n == p->steps - 1) ? 0.5 * eps : eps, p);
+    }
+  } else {
+    // Omelyan PQPQP: P(l eps) Q(eps/2) P((1-2l) eps) Q(eps/2) P(l eps); the
+    // closing and opening kicks of consecutive steps merge into P(2 l eps).
+    const double lam = p->lambda;
+    mom_update(ctx, P, U, U32, lam * eps, p);
+    for (int n = 0; n < p->steps; ++n) {
+      link_update(ctx, U, P, 0.5 * eps, p->reunitarize, U32, df);
+      mom_update(ctx, P, U, U32, (1.0 - 2.0 * lam) * eps, p);
+      link_update(ctx, U, P, 0.5 * eps, p->reunitarize, U32, df);
+      mom_update(ctx, P, U, U32, (n == p->steps - 1 ? 1.0 : 2.0) * lam * eps, p);
     }
   }
   r.V1 = potential(ctx, U, p);

@@ -46,9 +46,12 @@ extern "C" {
 #define GF_FP64 0  /* plain form: fp64 throughout */
 #define GF_MIXED 1 /* fp32 force and stout (12-real links), fp64 H / updates */
 
-/* integrators of the MD driver (molecular_dynamics.jl:604-616) */
+/* integrators of the MD driver (molecular_dynamics.jl:604-616); GF_OMELYAN is
+ * the second-order minimum-norm PQPQP scheme of the reference's custom
+ * integrator example OmelyanPQP(lambda) (docs/src/hmc.md:250-270) */
 #define GF_QPQ 0
 #define GF_PQP 1
+#define GF_OMELYAN 2
 
 #define GF_MAX_STOUT 4
 
@@ -64,7 +67,7 @@ typedef struct gf_md_params {
   double beta;           /* Wilson coupling */
   double tau;            /* trajectory_length, finite and nonzero */
   int steps;             /* > 0 */
-  int integrator;        /* GF_QPQ or GF_PQP */
+  int integrator;        /* GF_QPQ, GF_PQP or GF_OMELYAN */
   int precision;         /* GF_FP64 or GF_MIXED */
   int nstout;            /* 0 .. GF_MAX_STOUT smearing levels */
   double rho[GF_MAX_STOUT];
@@ -72,6 +75,7 @@ typedef struct gf_md_params {
   int stout_recompute;   /* 1: the adjoint recomputes each level's C_mu from the
                             stored level input instead of keeping it from the
                             forward pass (less memory, more flops) */
+  double lambda;         /* Omelyan parameter (GF_OMELYAN only) */
 } gf_md_params;
 
 /* ---- context ------------------------------------------------------------ */

@@ -938,7 +938,11 @@ double or_hamiltonian(const int L[4], const cdbl* U, const double* P, double bet
   return or_stout_action(L, U, nstout, rho, beta) + or_kinetic(L, P) / 2;
 }
 
-/* md_trajectory!: integrator 0 = QPQ, 1 = PQP; out = {H0, H1, dH} */
+static double g_omelyan_lambda = 0.1931833275037836;
+void or_set_omelyan_lambda(double lam) { g_omelyan_lambda = lam; }
+
+/* md_trajectory!: integrator 0 = QPQ, 1 = PQP, 2 = Omelyan PQPQP (the custom
+ * integrator of docs/src/hmc.md:250-270); out = {H0, H1, dH} */
 void or_md_trajectory(const int L[4], cdbl* U, double* P, double beta, double tau, int steps, int integrator,
                       int nstout, const double* rho, double* out) {
   Lat lat = mklat(L);
@@ -950,10 +954,17 @@ void or_md_trajectory(const int L[4], cdbl* U, double* P, double beta, double ta
       or_link_update(L, U, P, eps / 2);
       mom_update(L, P, U, eps, beta, nstout, rho, F);
       or_link_update(L, U, P, eps / 2);
-    } else {
+    } else if (integrator == 1) {
       mom_update(L, P, U, eps / 2, beta, nstout, rho, F);
       or_link_update(L, U, P, eps);
       mom_update(L, P, U, eps / 2, beta, nstout, rho, F);
+    } else {
+      double lam = g_omelyan_lambda;
+      mom_update(L, P, U, lam * eps, beta, nstout, rho, F);
+      or_link_update(L, U, P, eps / 2);
+      mom_update(L, P, U, (1 - 2 * lam) * eps, beta, nstout, rho, F);
+      or_link_update(L, U, P, eps / 2);
+      mom_update(L, P, U, lam * eps, beta, nstout, rho, F);
     }
   }
   double H1 = or_hamiltonian(L, U, P, beta, nstout, rho);

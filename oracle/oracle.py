@@ -55,6 +55,7 @@ def _declare(l):
         "or_set_threads": ([_I], None),
         "or_taylor_fallbacks": ([], ctypes.c_long),
         "or_set_exp_method": ([_I], None),
+        "or_set_omelyan_lambda": ([_D], None),
         "or_staple": ([_P, _P, _I, _P], None),
         "or_plaquette": ([_P, _P], _D),
         "or_dsdu": ([_P, _P, _D, _I, _P], None),
@@ -250,13 +251,14 @@ def hamiltonian(L, U, P, beta, rho=()):
     return lib().or_hamiltonian(_ptr(_L(L)), _ptr(U), _ptr(P), float(beta), len(rho), _ptr(r))
 
 
-def md_trajectory(L, U, P, beta, tau, steps, integrator="QPQ", rho=()):
-    """In place on U, P. Returns (H0, H1, dH)."""
+def md_trajectory(L, U, P, beta, tau, steps, integrator="QPQ", rho=(), lam=0.1931833275037836):
+    """In place on U, P. Returns (H0, H1, dH). integrator: QPQ, PQP or OMELYAN."""
     _chk(U, np.complex128)
     _chk(P, np.float64)
     out = np.zeros(3)
     r = _rho(rho)
-    integ = {"QPQ": 0, "PQP": 1}[integrator]
+    integ = {"QPQ": 0, "PQP": 1, "OMELYAN": 2}[integrator]
+    lib().or_set_omelyan_lambda(float(lam))
     lib().or_md_trajectory(_ptr(_L(L)), _ptr(U), _ptr(P), float(beta), float(tau), int(steps), integ, len(rho),
                            _ptr(r), _ptr(out))
     return tuple(out)

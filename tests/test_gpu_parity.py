@@ -152,6 +152,20 @@ def test_trajectory_config1(pkg, exact_exp_oracle, integrator):
     assert frob_mom(P.to_host(), Ph) < 1e-12
 
 
+def test_omelyan_trajectory(pkg, exact_exp_oracle):
+    """The reference's custom-integrator example OmelyanPQP(0.193...)."""
+    U = pkg.gauge_configuration(L8, start="hot", seed=21)
+    P = pkg.gaussian_momenta(U, seed=22)
+    Uh, Ph = U.to_host(), P.to_host()
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, 2.85, "plaquette")
+    drv = pkg.md_driver(U, action, steps=6, integrator=pkg.OmelyanPQP(0.1931833275037836), reunitarize=False)
+    res = pkg.md_trajectory_(U, P, drv)
+    h = exact_exp_oracle.md_trajectory(list(L8), Uh, Ph, 5.7, 1.0, 6, "OMELYAN")
+    assert abs(res.delta_hamiltonian - h[2]) <= 1e-10
+    assert frob_links(U.to_host(), Uh) < 1e-12
+
+
 def test_trajectory_config1_against_reference_eigen_exponential(pkg, oracle):
     """The same trajectory against the reference's own eigen-method exptU!.
     That method is accurate to ~1e-14 per update (its eigenvectors come from

@@ -138,6 +138,20 @@ def test_reversibility(oracle, integrator):
     assert np.abs(P - P0).max() < 2e-12
 
 
+def test_omelyan_is_reversible_and_second_order(oracle):
+    U0 = oracle.hot_start(L4, 1234)
+    P0 = oracle.gauss_mom(L4, 99)
+    U, P = U0.copy(), P0.copy()
+    oracle.md_trajectory(L4, U, P, 5.7, 1.0, 8, "OMELYAN")
+    oracle.md_trajectory(L4, U, P, 5.7, -1.0, 8, "OMELYAN")
+    assert np.abs(U - U0).max() < 2e-12 and np.abs(P - P0).max() < 2e-12
+    dh = []
+    for n in (8, 16):
+        U, P = U0.copy(), P0.copy()
+        dh.append(abs(oracle.md_trajectory(L4, U, P, 5.7, 1.0, n, "OMELYAN")[2]))
+    assert dh[0] / dh[1] == pytest.approx(4.0, rel=0.25)
+
+
 def test_delta_h_scales_as_eps_squared(oracle):
     U0 = oracle.hot_start(L4, 1234)
     P0 = oracle.gauss_mom(L4, 99)
