@@ -26,14 +26,12 @@ namespace dfns {
 
 struct dfl {
   float hi, lo;
-  GF_DF_HD dfl() : hi(0.f), lo(0.f) {}
-  GF_DF_HD dfl(float h, float l) : hi(h), lo(l) {}
-  GF_DF_HD dfl(int v) : hi((float)v), lo(0.f) {}
-  GF_DF_HD explicit dfl(float v) : hi(v), lo(0.f) {}
-  GF_DF_HD explicit dfl(double v) {
-    hi = (float)v;
-    lo = (float)(v - (double)hi);
-  }
+  GF_DF_HD constexpr dfl() : hi(0.f), lo(0.f) {}
+  GF_DF_HD constexpr dfl(float h, float l) : hi(h), lo(l) {}
+  GF_DF_HD constexpr dfl(int v) : hi((float)v), lo(0.f) {}
+  GF_DF_HD constexpr explicit dfl(float v) : hi(v), lo(0.f) {}
+  // constexpr so that literal constants are split at compile time
+  GF_DF_HD constexpr explicit dfl(double v) : hi((float)v), lo((float)(v - (double)(float)v)) {}
   GF_DF_HD explicit operator double() const { return (double)hi + (double)lo; }
 };
 
@@ -128,6 +126,20 @@ __device__ __forceinline__ dfl df_from_double(double d) {
   return dfl(hi, sign ? -lo : lo);
 }
 
-__device__ __forceinline__ double df_to_double(dfl a) { return (double)a.hi + (double)a.lo; }
+// fp32 -> fp64 widening with integer operations. Zero and subnormal parts
+// (only ever the lo part of a value below 2^-100) map to zero; infinities and
+// NaN take the fp64 conversion so that they propagate.
+__device__ __forceinline__ double widen_f32(float f) {
+  unsigned int b = (unsigned int)__float_as_int(f);
+  unsigned int e = (b >> 23) & 0xFFu;
+  if (e == 0u) return 0.0;
+  if (e == 0xFFu) return (double)f;
+  unsigned long long d = ((unsigned long long)(b >> 31) << 63) | ((unsigned long long)(e - 127u + 1023u) << 52) |
+                         ((unsigned long long)(b & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)d);
+}
+
+// hi + lo as fp64: two integer widenings and one fp64 add
+__device__ __forceinline__ double df_to_double(dfl a) { return widen_f32(a.hi) + widen_f32(a.lo); }
 
 }  // namespace gf

@@ -206,7 +206,8 @@ GF_HD cplx<R> tr_nn(const mat3<R>& a, const mat3<R>& b) {
 template <typename R>
 GF_HD mat3<R> ta_proj(const mat3<R>& m) {
   mat3<R> y;
-  R tri = (m.e[0][0].im + m.e[1][1].im + m.e[2][2].im) * (R(1) / R(3));
+  constexpr R third = R(1.0 / 3.0), half = R(0.5), mhalf = R(-0.5);
+  R tri = (m.e[0][0].im + m.e[1][1].im + m.e[2][2].im) * third;
 #pragma unroll
   for (int i = 0; i < 3; ++i) y.e[i][i] = mk<R>(R(0), m.e[i][i].im - tri);
 #pragma unroll
@@ -214,8 +215,8 @@ GF_HD mat3<R> ta_proj(const mat3<R>& m) {
 #pragma unroll
     for (int j = i + 1; j < 3; ++j) {
       cplx<R> x = m.e[i][j] - conj(m.e[j][i]);
-      y.e[i][j] = R(0.5) * x;
-      y.e[j][i] = mk<R>(R(-0.5) * x.re, R(0.5) * x.im);
+      y.e[i][j] = half * x;
+      y.e[j][i] = mk<R>(mhalf * x.re, half * x.im);
     }
   return y;
 }
@@ -225,7 +226,7 @@ GF_HD mat3<R> ta_proj(const mat3<R>& m) {
 // Traceless_antihermitian_add! for NC = 3.
 template <typename R>
 GF_HD void ta_coeffs(const mat3<R>& m, R c[8]) {
-  const R sr3i = R(0.57735026918962576451);  // 1/sqrt(3)
+  constexpr R sr3i = R(0.57735026918962576451);  // 1/sqrt(3)
   // off-diagonal: x_ij = M_ij - conj(M_ji) = 2 y_ij
   cplx<R> x12 = m.e[0][1] - conj(m.e[1][0]);
   cplx<R> x13 = m.e[0][2] - conj(m.e[2][0]);
@@ -244,12 +245,12 @@ GF_HD void ta_coeffs(const mat3<R>& m, R c[8]) {
 // Hermitian matrix Q = sum_a p_a lambda_a / 2 (Gell-Mann basis).
 template <typename R>
 GF_HD mat3<R> herm_from_coeffs(const R p[8]) {
-  const R sr3i = R(0.57735026918962576451);
+  constexpr R sr3i = R(0.57735026918962576451);
+  constexpr R h = R(0.5), two = R(2.0);
   mat3<R> q;
-  R h = R(0.5);
   q.e[0][0] = mk<R>(h * (p[2] + sr3i * p[7]), R(0));
   q.e[1][1] = mk<R>(h * (-p[2] + sr3i * p[7]), R(0));
-  q.e[2][2] = mk<R>(-h * R(2) * sr3i * p[7], R(0));
+  q.e[2][2] = mk<R>(-h * two * sr3i * p[7], R(0));
   q.e[0][1] = mk<R>(h * p[0], -h * p[1]);
   q.e[1][0] = mk<R>(h * p[0], h * p[1]);
   q.e[0][2] = mk<R>(h * p[3], -h * p[4]);
@@ -493,7 +494,8 @@ GF_HD void herm_invariants(const mat3<R>& q, R& c0, R& c1) {
   R a12 = q12.re * q12.re + q12.im * q12.im;
   R a13 = q13.re * q13.re + q13.im * q13.im;
   R a23 = q23.re * q23.re + q23.im * q23.im;
-  c1 = R(0.5) * (q11 * q11 + q22 * q22 + q33 * q33) + a12 + a13 + a23;
+  constexpr R half = R(0.5);
+  c1 = half * (q11 * q11 + q22 * q22 + q33 * q33) + a12 + a13 + a23;
   // det = q11 q22 q33 + 2 Re(q12 q23 q31) - q11|q23|^2 - q22|q13|^2 - q33|q12|^2
   cplx<R> t = q12 * q23;
   R re3 = t.re * q13.re + t.im * q13.im;  // Re(q12 q23 conj(q13))
@@ -556,7 +558,7 @@ GF_HD dfl dacc_get(const dacc& a) { return df_two_sum(a.s, a.c); }
 template <bool DA, bool DB, bool ACC>
 GF_HD mat3<dfl> df_matmul(const mat3<dfl>& a, const mat3<dfl>& b, const mat3<dfl>* c) {
   mat3<dfl> r;
-#pragma unroll
+#pragma unroll 1
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
