@@ -143,6 +143,7 @@ extern "C" int gf_ctx_destroy(gf_ctx* ctx) {
   if (ctx->d_result) cudaFree(ctx->d_result);
   if (ctx->h_result) cudaFreeHost(ctx->h_result);
   if (ctx->d_hash) cudaFree(ctx->d_hash);
+  if (ctx->d_stage) cudaFree(ctx->d_stage);
   if (ctx->h_hash) cudaFreeHost(ctx->h_hash);
   if (ctx->prof_ev) {
     for (int i = 0; i < 2 * GF_PROF_CAP; ++i) cudaEventDestroy(ctx->prof_ev[i]);

@@ -183,14 +183,24 @@ __global__ void k_mom_to_ref(const double* __restrict__ in, double* __restrict__
   for (int a = 0; a < 8; ++a) dst[a] = in[((size_t)mu * 8 + a) * g.vol + s];
 }
 
+// One staging buffer per context, kept between transfers (a fresh 0.6 GB
+// allocation per call cost more than the copy itself).
 static void* staging(gf_ctx* ctx, size_t bytes) {
-  void* p = nullptr;
-  cudaError_t e = cudaMallocAsync(&p, bytes, ctx->stream);
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    throw gf_error(GF_ENOMEM, std::string("staging allocation failed: ") + cudaGetErrorString(e));
+  if (ctx->stage_bytes < bytes) {
+    if (ctx->d_stage) {
+      GF_CUDA(cudaStreamSynchronize(ctx->stream));
+      cudaFree(ctx->d_stage);
+      ctx->d_stage = nullptr;
+      ctx->stage_bytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&ctx->d_stage, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      throw gf_error(GF_ENOMEM, std::string("staging allocation failed: ") + cudaGetErrorString(e));
+    }
+    ctx->stage_bytes = bytes;
   }
-  return p;
+  return ctx->d_stage;
 }
 
 static void require_kind(const gf_field* f, int k1, int k2, const char* what) {
@@ -206,7 +216,6 @@ void upload_links(gf_ctx* ctx, gf_field* U, const double* host) {
   dim3 grid(blocks_for(ctx->geom.vol, 256), 4);
   k_links_from_ref<<<grid, 256, 0, ctx->stream>>>((const double2*)tmp, (double2*)U->ptr, ctx->geom);
   GF_CHECK_LAUNCH();
-  GF_CUDA(cudaFreeAsync(tmp, ctx->stream));
   GF_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
@@ -218,7 +227,6 @@ void download_links(gf_ctx* ctx, const gf_field* U, double* host) {
   k_links_to_ref<<<grid, 256, 0, ctx->stream>>>((const double2*)U->ptr, (double2*)tmp, ctx->geom);
   GF_CHECK_LAUNCH();
   GF_CUDA(cudaMemcpyAsync(host, tmp, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-  GF_CUDA(cudaFreeAsync(tmp, ctx->stream));
   GF_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
@@ -230,7 +238,6 @@ void upload_mom(gf_ctx* ctx, gf_field* P, const double* host) {
   dim3 grid(blocks_for(ctx->geom.vol, 256), 4);
   k_mom_from_ref<<<grid, 256, 0, ctx->stream>>>((const double*)tmp, (double*)P->ptr, ctx->geom);
   GF_CHECK_LAUNCH();
-  GF_CUDA(cudaFreeAsync(tmp, ctx->stream));
   GF_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
@@ -242,7 +249,6 @@ void download_mom(gf_ctx* ctx, const gf_field* P, double* host) {
   k_mom_to_ref<<<grid, 256, 0, ctx->stream>>>((const double*)P->ptr, (double*)tmp, ctx->geom);
   GF_CHECK_LAUNCH();
   GF_CUDA(cudaMemcpyAsync(host, tmp, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-  GF_CUDA(cudaFreeAsync(tmp, ctx->stream));
   GF_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 

@@ -75,6 +75,9 @@ struct gf_ctx {
   double vc_V, vc_beta;
   int vc_nstout, vc_precision;
   double vc_rho[GF_MAX_STOUT];
+  // staging buffer for host transfers in the reference layout (grown on demand)
+  void* d_stage;
+  size_t stage_bytes;
   // per-kernel CUDA-event timing on the context's stream (gf_prof_*)
   int prof_on;
   int prof_n;

@@ -558,7 +558,10 @@ GF_HD dfl dacc_get(const dacc& a) { return df_two_sum(a.s, a.c); }
 template <bool DA, bool DB, bool ACC>
 GF_HD mat3<dfl> df_matmul(const mat3<dfl>& a, const mat3<dfl>& b, const mat3<dfl>* c) {
   mat3<dfl> r;
-#pragma unroll 1
+  // Keep all three loops unrolled: a rolled row loop (unroll 1) compiled to
+  // wrong staple sums inside the double-float stout kernels, although each
+  // product alone was correct.
+#pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
