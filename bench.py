@@ -75,10 +75,13 @@ def algorithmic_flops_per_link(kclass):
     mm, mac, rec = 198, 216, 42
     staples = 6 * (mm + mac)  # six staples, two products each
     base = _base(kclass)
+    full = kclass.endswith("64") or kclass.endswith("_df")  # 18-real links: nothing to rebuild
     return {
         "stout_fwd": staples + 2 * mm + 600,             # + U S, exp (series + Qh^2), E U
         "bwd_local": (staples / 2.0) + 8 * mm + 900,     # mean: top level rebuilds staples
-        "bwd_gather": 3 * 6 * (mm + mac) + 18 * rec + mm / 2.0,
+        # per axis 4 products + 6 accumulated products (the 18 staple-position
+        # terms factored), 6 links rebuilt from 12 reals; bottom level: U D
+        "bwd_gather": 3 * (4 * mm + 6 * mac) + (0 if full else 18 * rec) + mm / 2.0,
         "link_update": 2 * mm + 400,
         "plaquette": 2 * mm * 6 / 4.0,
         "force": staples + mm,
@@ -289,8 +292,8 @@ def e2e_hmc(pkg, torch, L, steps, warmup, rank):
             "d2h_bytes_per_step": 36 * V * 16 + 3 * 8, "ms_per_step": 1e3 * sec / steps}
 
 
-def dh_check(pkg, L, ntherm):
-    """|Delta H_mixed - Delta H_fp64| for one trajectory from the same
+def dh_check(pkg, L, ntherm, forms=("fp64", "mixed")):
+    """|Delta H_form - Delta H_fp64| for one trajectory from the same
     configuration and momenta. The configuration is thermalised first: cold
     start, then `ntherm` mixed-precision trajectories kept unconditionally."""
     U, P, drv = make_setup(pkg, L, "mixed", SEED)
@@ -301,14 +304,18 @@ def dh_check(pkg, L, ntherm):
     Ut = U.to_host()
     plaq = pkg.measure_plaquette(U)
     res = {}
-    for prec in ("fp64", "mixed"):
+    for prec in forms:
         U2, P2, drv2 = make_setup(pkg, L, prec, SEED)
         U2.from_host(Ut)
         pkg.gaussian_momenta_(P2, seed=SEED, sweep=10 ** 6)
         res[prec] = pkg.md_trajectory_(U2, P2, drv2).delta_hamiltonian
         del U2, P2, drv2
-    return {"dH_fp64": res["fp64"], "dH_mixed": res["mixed"], "abs_diff": abs(res["mixed"] - res["fp64"]),
-            "start": "cold start + %d mixed trajectories kept unconditionally (plaquette %.6f)" % (ntherm, plaq)}
+    out = {"dH_fp64": res["fp64"], "dH_mixed": res["mixed"], "abs_diff": abs(res["mixed"] - res["fp64"])}
+    if "dfloat" in res:
+        out["dH_dfloat"] = res["dfloat"]
+        out["abs_diff_dfloat"] = abs(res["dfloat"] - res["fp64"])
+    out["start"] = "cold start + %d mixed trajectories kept unconditionally (plaquette %.6f)" % (ntherm, plaq)
+    return out
 
 
 def oracle_sample(threads, L_sample=16, md_steps=None):
@@ -595,6 +602,7 @@ def main():
     ap.add_argument("--lattice", type=int, default=32)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-dfloat", action="store_true", help="skip the double-float form's line")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--therm", type=int, default=10, help="thermalisation trajectories before the Delta H check")
     ap.add_argument("--mode", default="hmc", choices=["hmc", "force", "link", "precision", "wilson", "scale"],
@@ -646,7 +654,17 @@ def main():
         s64, _, _, _, _ = timed_hmc(pkg, torch, U, P, drv, 1, 1, rank, None)
         fp64 = {"value": 1.0 / s64, "unit": UNIT, "ms_per_step": 1e3 * s64, "steps": 1, "warmup": 1}
         del U, P, drv
-    dh = dh_check(pkg, L, args.therm) if not args.no_fp64 else None
+    # double-float form: force, stout adjoint and link updates in fp32-pair
+    # arithmetic on fp64 links
+    dflt = None
+    if not args.no_dfloat:
+        U, P, drv = make_setup(pkg, L, "dfloat", SEED + 101 * rank)
+        sdf, _, kdf, _, _ = timed_hmc(pkg, torch, U, P, drv, 2, 1, rank, None, prof=True)
+        dflt = {"value": 2.0 / sdf, "unit": UNIT, "ms_per_step": 1e3 * sdf / 2, "steps": 2, "warmup": 1,
+                "kernels_ms_per_step": {k: v["ms"] / 2 for k, v in kdf.items()}}
+        del U, P, drv
+    forms = ("fp64", "mixed") + (() if args.no_dfloat else ("dfloat",))
+    dh = dh_check(pkg, L, args.therm, forms) if not args.no_fp64 else None
 
     e2e = None
     if not args.no_e2e:
@@ -695,6 +713,8 @@ def main():
             "e2e": e2e, "gpu_launches": launches, "roofline": roof, "compute": compute, "cpu_baseline": cpu,
             "clocks": clocks, "fp64_form": fp64,
             "mixed_over_fp64": (value / world) / fp64["value"] if fp64 else None,
+            "dfloat_form": dflt,
+            "dfloat_over_fp64": dflt["value"] / fp64["value"] if (fp64 and dflt) else None,
             "dH_check": dh, "kernels": kern, "gemm_peaks": peaks,
             "accepted": acc, "dH_timed": dhs,
         }

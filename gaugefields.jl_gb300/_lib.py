@@ -17,7 +17,7 @@ GF_ENAN = -4
 GF_ESTATE = -5
 
 GF_LINK64, GF_LINK32, GF_MOM64, GF_MAT64, GF_MAT32 = 1, 2, 3, 4, 5
-GF_FP64, GF_MIXED = 0, 1
+GF_FP64, GF_MIXED, GF_DFLOAT = 0, 1, 2
 GF_QPQ, GF_PQP, GF_OMELYAN = 0, 1, 2
 GF_MAX_STOUT = 4
 
@@ -86,6 +86,8 @@ SIGNATURES = {
     "gf_link_update": [_P, _P, _P, _D, _I],
     "gf_hamiltonian": [_P, _P, _P, ctypes.POINTER(MDParams), _DP],
     "gf_md_trajectory": [_P, _P, _P, ctypes.POINTER(MDParams), _DP],
+    "gf_md_mom_update": [_P, _P, _P, _D, ctypes.POINTER(MDParams)],
+    "gf_md_link_update": [_P, _P, _P, _D, ctypes.POINTER(MDParams)],
     "gf_hmc_update": [_P, _P, _P, ctypes.POINTER(MDParams), _U64, _U64, _D, _DP],
     "gf_stout_create": [_P, _I, _DP, _I, _I, ctypes.POINTER(_P)],
     "gf_stout_destroy": [_P],
@@ -101,11 +103,13 @@ SIGNATURES = {
 }
 
 KERNEL_CLASSES = ["plaquette", "force", "link_update", "stout_fwd", "bwd_local", "bwd_gather", "stout_fwd64",
-                  "bwd_local64", "bwd_gather64", "other", "link_update_df", "stout_fwd_df"]
+                  "bwd_local64", "bwd_gather64", "other", "link_update_df", "stout_fwd_df", "force_df",
+                  "bwd_local_df", "bwd_gather_df"]
 # arithmetic precision of each class (the force class follows its links)
 KERNEL_PRECISION = {"plaquette": "fp64", "force": "fp32", "link_update": "fp64", "stout_fwd": "fp32",
                     "bwd_local": "fp32", "bwd_gather": "fp32", "stout_fwd64": "fp64", "bwd_local64": "fp64",
-                    "bwd_gather64": "fp64", "other": "fp64", "link_update_df": "df", "stout_fwd_df": "df"}
+                    "bwd_gather64": "fp64", "other": "fp64", "link_update_df": "df", "stout_fwd_df": "df",
+                    "force_df": "df", "bwd_local_df": "df", "bwd_gather_df": "df"}
 
 _lib = None
 

@@ -347,6 +347,9 @@ class OmelyanPQP:
         self.lam = float(lam)
 
 
+_PRECISION = {"fp64": _lib.GF_FP64, "mixed": _lib.GF_MIXED, "dfloat": _lib.GF_DFLOAT}
+
+
 class MDDriver:
     def __init__(self, action, integrator, trajectory_length, steps, smearing, precision, reunitarize,
                  recompute=False):
@@ -358,7 +361,6 @@ class MDDriver:
         self.precision = precision
         self.reunitarize = reunitarize
         self.recompute = recompute
-        self._stout = None
 
     def params(self):
         p = MDParams()
@@ -370,7 +372,7 @@ class MDDriver:
             p.lam = self.integrator.lam
         else:
             p.integrator = _lib.GF_PQP if isinstance(self.integrator, PQP) else _lib.GF_QPQ
-        p.precision = _lib.GF_MIXED if self.precision == "mixed" else _lib.GF_FP64
+        p.precision = _PRECISION[self.precision]
         rho = self.smearing.rhos() if self.smearing is not None else []
         p.nstout = len(rho)
         for i, r in enumerate(rho):
@@ -386,8 +388,10 @@ def md_driver(U, action, steps, trajectory_length=1.0, integrator=None, smearing
 
     smearing: a CovNeuralnet of stout layers; the action is then evaluated on
     the smeared links and the force is back-propagated to the thin links.
-    precision: "fp64" (plain form) or "mixed" (fp32 force and stout on 12-real
-    links; fp64-class Hamiltonian, Delta H, link updates and re-unitarisation).
+    precision: "fp64" (plain form), "mixed" (fp32 force and stout on 12-real
+    links; fp64-class Hamiltonian, Delta H, link updates and re-unitarisation)
+    or "dfloat" (force, stout and link updates in double-float arithmetic on
+    the fp32 pipes, fp64 links; fp64 Hamiltonian).
     recompute: the stout adjoint rebuilds each level's staple sum C instead of
     keeping it from the forward pass (less device memory)."""
     integrator = integrator if integrator is not None else QPQ()
@@ -399,8 +403,8 @@ def md_driver(U, action, steps, trajectory_length=1.0, integrator=None, smearing
         raise ValueError("trajectory_length must be finite; got %s" % trajectory_length)
     if trajectory_length == 0:
         raise ValueError("trajectory_length must not be zero")
-    if precision not in ("fp64", "mixed"):
-        raise ValueError("precision must be 'fp64' or 'mixed'")
+    if precision not in _PRECISION:
+        raise ValueError("precision must be 'fp64', 'mixed' or 'dfloat'")
     if not (isinstance(integrator, (QPQ, PQP, OmelyanPQP)) or callable(integrator)):
         raise ValueError("md_step! is not implemented for %s" % type(integrator).__name__)
     if not isinstance(action, GaugeAction) or not action.terms:
@@ -441,38 +445,24 @@ def md_hamiltonian(U, P, driver):
 
 
 def update_gaugefields_(U, P, step_size, driver):
-    """U_mu <- exp(step_size P_mu) U_mu (molecular_dynamics.jl:513-531)."""
+    """U_mu <- exp(step_size P_mu) U_mu (molecular_dynamics.jl:513-531), in the
+    driver's precision (double-float for the mixed and double-float forms)."""
     if not math.isfinite(step_size):
         raise ValueError("the gauge-field step size must be finite; got %s" % step_size)
-    call("gf_link_update", U.ctx.h, U.field.h, P.field.h, ctypes.c_double(step_size),
-         1 if driver.reunitarize else 0, ctx=U.ctx.h)
+    p = driver.params()
+    call("gf_md_link_update", U.ctx.h, U.field.h, P.field.h, ctypes.c_double(step_size), ctypes.byref(p),
+         ctx=U.ctx.h)
     return U
 
 
-def _stout_for(driver, U):
-    if driver._stout is None:
-        driver._stout = _StoutStack(U.ctx, driver.smearing.rhos(), driver.precision, store=not driver.recompute)
-    return driver._stout
-
-
 def update_momenta_(P, U, step_size, driver):
-    """P <- P + step_size * F(U) (molecular_dynamics.jl:539-551)."""
+    """P <- P + step_size * F(U) (molecular_dynamics.jl:539-551) with the
+    driver's action, smearing and precision."""
     if not math.isfinite(step_size):
         raise ValueError("the momentum step size must be finite; got %s" % step_size)
-    beta = driver.action.beta
-    if driver.smearing is None and driver.precision == "fp64":
-        call("gf_mom_update", U.ctx.h, P.field.h, U.field.h, ctypes.c_double(step_size), ctypes.c_double(beta),
-             ctx=U.ctx.h)
-    elif driver.smearing is None:
-        # mixed precision without smearing: fp32 12-real copy of the links
-        st = driver.__dict__.setdefault("_u32", Gaugefields4D(U.ctx, _lib.GF_LINK32))
-        call("gf_field_copy", U.ctx.h, st.field.h, U.field.h, ctx=U.ctx.h)
-        call("gf_mom_update", U.ctx.h, P.field.h, st.field.h, ctypes.c_double(step_size), ctypes.c_double(beta),
-             ctx=U.ctx.h)
-    else:
-        stack = _stout_for(driver, U)
-        call("gf_stout_mom_update", U.ctx.h, stack.h, P.field.h, U.field.h, ctypes.c_double(step_size),
-             ctypes.c_double(beta), ctx=U.ctx.h)
+    p = driver.params()
+    call("gf_md_mom_update", U.ctx.h, P.field.h, U.field.h, ctypes.c_double(step_size), ctypes.byref(p),
+         ctx=U.ctx.h)
     return P
 
 
@@ -582,7 +572,7 @@ class _StoutStack:
         self.ctx = ctx
         arr = (ctypes.c_double * len(rhos))(*rhos)
         h = ctypes.c_void_p()
-        prec = _lib.GF_MIXED if precision == "mixed" else _lib.GF_FP64
+        prec = _PRECISION[precision]
         call("gf_stout_create", ctx.h, len(rhos), arr, prec, 1 if store else 0, ctypes.byref(h), ctx=ctx.h)
         self.h = h
         self.precision = precision

@@ -35,6 +35,17 @@ struct dfl {
   GF_DF_HD explicit operator double() const { return (double)hi + (double)lo; }
 };
 
+// The rounded product fl(a*b) as a value the compiler cannot fuse into a
+// following add (nvcc contracts a*b + c into one FMA by default, which would
+// make the error-free transformations below count the product error twice).
+GF_DF_HD float df_mul_rn(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+
 GF_DF_HD dfl df_two_sum(float a, float b) {
   float s = a + b;
   float bb = s - a;
@@ -47,7 +58,7 @@ GF_DF_HD dfl df_fast_two_sum(float a, float b) {
   return dfl(s, e);
 }
 GF_DF_HD dfl df_two_prod(float a, float b) {
-  float p = a * b;
+  float p = df_mul_rn(a, b);
   float e = fmaf(a, b, -p);
   return dfl(p, e);
 }
@@ -64,7 +75,7 @@ GF_DF_HD dfl operator-(dfl a) { return dfl(-a.hi, -a.lo); }
 GF_DF_HD dfl operator-(dfl a, dfl b) { return a + (-b); }
 GF_DF_HD dfl operator*(dfl a, dfl b) {
   dfl p = df_two_prod(a.hi, b.hi);
-  float t = fmaf(a.hi, b.lo, a.lo * b.hi);
+  float t = fmaf(a.hi, b.lo, df_mul_rn(a.lo, b.hi));
   return df_fast_two_sum(p.hi, p.lo + t);
 }
 GF_DF_HD dfl operator/(dfl a, dfl b) {
@@ -103,6 +114,7 @@ using dfns::dfl;
 using dfns::df_two_sum;
 using dfns::df_fast_two_sum;
 using dfns::df_two_prod;
+using dfns::df_mul_rn;
 
 // Split an fp64 value into hi + lo fp32 parts with integer operations only:
 // hi keeps the sign, exponent and leading 23 fraction bits (truncated), lo the
@@ -141,5 +153,10 @@ __device__ __forceinline__ double widen_f32(float f) {
 
 // hi + lo as fp64: two integer widenings and one fp64 add
 __device__ __forceinline__ double df_to_double(dfl a) { return widen_f32(a.hi) + widen_f32(a.lo); }
+
+// a kernel result of any arithmetic type as fp64
+__device__ __forceinline__ double to_f64(double v) { return v; }
+__device__ __forceinline__ double to_f64(float v) { return (double)v; }
+__device__ __forceinline__ double to_f64(dfl v) { return df_to_double(v); }
 
 }  // namespace gf

@@ -347,10 +347,11 @@ extern "C" int gf_staple(gf_ctx* ctx, const gf_field* U, int mu, gf_field* V) {
 // ---------------------------------------------------------------------------
 // stout workspace
 // ---------------------------------------------------------------------------
-static gf_stout* stout_new(gf_ctx* ctx, int nlev, const double* rho, int precision, int store) {
+static gf_stout* stout_new(gf_ctx* ctx, int nlev, const double* rho, int precision, int store,
+                           bool fwd_only = false) {
   need(nlev >= 1 && nlev <= GF_MAX_STOUT, "stout: number of levels must be 1..GF_MAX_STOUT");
-  need(precision == GF_FP64 || precision == GF_MIXED || precision == GF_PREC_DF,
-       "stout: precision must be GF_FP64 or GF_MIXED");
+  need(precision == GF_FP64 || precision == GF_MIXED || precision == GF_DFLOAT,
+       "stout: precision must be GF_FP64, GF_MIXED or GF_DFLOAT");
   for (int l = 0; l < nlev; ++l) need(std::isfinite(rho[l]), "stout: rho must be finite");
   gf_stout* st = new gf_stout();
   st->ctx = ctx;
@@ -362,8 +363,9 @@ static gf_stout* stout_new(gf_ctx* ctx, int nlev, const double* rho, int precisi
   int mk = precision == GF_MIXED ? GF_MAT32 : GF_MAT64;
   try {
     for (int l = 1; l <= nlev; ++l) st->lev_in[l] = field_new(ctx, lk);
-    if (precision == GF_PREC_DF) {
+    if (fwd_only) {
       st->store = 0;  // forward only: no C, no back-propagation buffers
+      st->fwd_only = 1;
       return st;
     }
     if (st->store)
@@ -382,7 +384,8 @@ static gf_stout* stout_new(gf_ctx* ctx, int nlev, const double* rho, int precisi
 extern "C" int gf_stout_create(gf_ctx* ctx, int nlev, const double* rho, int precision, int store, gf_stout** out) {
   API_BEGIN
   need(ctx && rho && out, "gf_stout_create: null argument");
-  need(precision == GF_FP64 || precision == GF_MIXED, "gf_stout_create: precision must be GF_FP64 or GF_MIXED");
+  need(precision == GF_FP64 || precision == GF_MIXED || precision == GF_DFLOAT,
+       "gf_stout_create: precision must be GF_FP64, GF_MIXED or GF_DFLOAT");
   *out = stout_new(ctx, nlev, rho, precision, store);
   API_END(ctx)
 }
@@ -443,36 +446,42 @@ static void check_md(const gf_md_params* p) {
   need(p->integrator == GF_QPQ || p->integrator == GF_PQP || p->integrator == GF_OMELYAN,
        "md: integrator must be GF_QPQ, GF_PQP or GF_OMELYAN");
   need(p->integrator != GF_OMELYAN || std::isfinite(p->lambda), "md: the Omelyan lambda must be finite");
-  need(p->precision == GF_FP64 || p->precision == GF_MIXED, "md: precision must be GF_FP64 or GF_MIXED");
+  need(p->precision == GF_FP64 || p->precision == GF_MIXED || p->precision == GF_DFLOAT,
+       "md: precision must be GF_FP64, GF_MIXED or GF_DFLOAT");
   need(p->nstout >= 0 && p->nstout <= GF_MAX_STOUT, "md: nstout must be 0..GF_MAX_STOUT");
   for (int l = 0; l < p->nstout; ++l) need(std::isfinite(p->rho[l]), "md: rho must be finite");
 }
 
+// The context's stack for a stack precision. The mixed form's Hamiltonian
+// uses a forward-only double-float stack; the GF_DFLOAT form shares one full
+// double-float stack between its force and its Hamiltonian.
 static gf_stout* ctx_stout(gf_ctx* ctx, const gf_md_params* p, int precision) {
   gf_stout** slot = precision == GF_FP64 ? &ctx->w_stout64
                     : (precision == GF_MIXED ? &ctx->w_stout32 : &ctx->w_stoutdf);
-  int store = (precision == GF_PREC_DF) ? 0 : (p->stout_recompute ? 0 : 1);
-  bool same = *slot && (*slot)->nlev == p->nstout && (*slot)->store == store;
+  const bool fwd_only = precision == GF_PREC_DF && p->precision == GF_MIXED;
+  int store = fwd_only ? 0 : (p->stout_recompute ? 0 : 1);
+  bool same = *slot && (*slot)->nlev == p->nstout && (*slot)->store == store && (*slot)->fwd_only == (int)fwd_only;
   if (same)
     for (int l = 0; l < p->nstout; ++l) same = same && (*slot)->rho[l] == p->rho[l];
   if (!same) {
     if (*slot) gf_stout_destroy(*slot);
     *slot = nullptr;
-    *slot = stout_new(ctx, p->nstout, p->rho, precision, store);
+    *slot = stout_new(ctx, p->nstout, p->rho, precision, store, fwd_only);
   }
   return *slot;
 }
 
 // The potential on the (smeared) fp64 links. The plain form evaluates it in
-// fp64. The mixed form smears in double-float arithmetic (~1e-14 per
-// operation, compensated products) on the fp32 pipes with fp64 storage, which
-// on GB300 is 2.1x faster than the fp64 stout forward; the plaquette sum over
-// the smeared links stays fp64 (GF_DF_HAMILTONIAN=0 keeps everything fp64).
+// fp64. The mixed and double-float forms smear in double-float arithmetic
+// (~1e-14 per operation, compensated products) on the fp32 pipes with fp64
+// storage, which on GB300 is 2.1x faster than the fp64 stout forward; the
+// plaquette sum over the smeared links stays fp64 (GF_DF_HAMILTONIAN=0 keeps
+// the mixed form's potential fp64).
 #ifndef GF_DF_HAMILTONIAN
 #define GF_DF_HAMILTONIAN 1
 #endif
 static double potential(gf_ctx* ctx, const gf_field* U, const gf_md_params* p) {
-  bool df = GF_DF_HAMILTONIAN && p->precision == GF_MIXED;
+  bool df = (GF_DF_HAMILTONIAN && p->precision == GF_MIXED) || p->precision == GF_DFLOAT;
   if (p->nstout == 0) return -(p->beta / 3.0) * plaquette_sum(ctx, U);
   gf_stout* st = ctx_stout(ctx, p, df ? GF_PREC_DF : GF_FP64);
   stout_forward(ctx, st, U, nullptr);
@@ -489,10 +498,10 @@ static void mom_update(gf_ctx* ctx, gf_field* P, const gf_field* U, const gf_fie
                        const gf_md_params* p) {
   const gf_field* links = (p->precision == GF_MIXED) ? U32 : U;
   if (p->nstout == 0) {
-    wilson_force_coef(ctx, links, P, eps * (-1.0 / 3.0) * (0.5 * p->beta), 1.0);
+    wilson_force_coef(ctx, links, P, eps * (-1.0 / 3.0) * (0.5 * p->beta), 1.0, p->precision == GF_DFLOAT);
     return;
   }
-  gf_stout* st = ctx_stout(ctx, p, p->precision == GF_MIXED ? GF_MIXED : GF_FP64);
+  gf_stout* st = ctx_stout(ctx, p, p->precision);
   stout_forward(ctx, st, links, nullptr);
   stout_backward(ctx, st, nullptr, p->beta, nullptr, P, eps);
 }
@@ -545,7 +554,7 @@ static MDResult md_run(gf_ctx* ctx, gf_field* U, gf_field* P, const gf_md_params
   // _md_fast_qpq! does (molecular_dynamics.jl:618-633): n+1 link updates and
   // n forces (QPQ), or n+1 forces and n link updates (PQP). The trajectory
   // is the one of md_step! up to rounding.
-  const bool df = p->precision == GF_MIXED;  // link updates in double-float
+  const bool df = p->precision != GF_FP64;  // link updates in double-float
   if (p->integrator == GF_QPQ) {
     link_update(ctx, U, P, 0.5 * eps, p->reunitarize, U32, df);
     for (int n = 0; n < p->steps; ++n) {
@@ -617,6 +626,38 @@ extern "C" int gf_hamiltonian(gf_ctx* ctx, const gf_field* U, const gf_field* P,
   need_kind(U, GF_LINK64, "gf_hamiltonian: U");
   need_kind(P, GF_MOM64, "gf_hamiltonian: P");
   *out = hamiltonian(ctx, U, P, prm);
+  API_END(ctx)
+}
+
+extern "C" int gf_md_mom_update(gf_ctx* ctx, gf_field* P, const gf_field* U, double eps, const gf_md_params* prm) {
+  API_BEGIN
+  need(ctx && U && P, "gf_md_mom_update: null argument");
+  need_ctx(ctx, U);
+  need_ctx(ctx, P);
+  check_md(prm);
+  need_kind(U, GF_LINK64, "gf_md_mom_update: U");
+  need_kind(P, GF_MOM64, "gf_md_mom_update: P");
+  need(std::isfinite(eps), "gf_md_mom_update: the momentum step size must be finite");
+  gf_field* U32 = nullptr;
+  if (prm->precision == GF_MIXED) {
+    if (!ctx->w_link32) ctx->w_link32 = field_new(ctx, GF_LINK32);
+    U32 = ctx->w_link32;
+    link64_to_32(ctx, U32, U);
+  }
+  mom_update(ctx, P, U, U32, eps, prm);
+  API_END(ctx)
+}
+
+extern "C" int gf_md_link_update(gf_ctx* ctx, gf_field* U, const gf_field* P, double eps, const gf_md_params* prm) {
+  API_BEGIN
+  need(ctx && U && P, "gf_md_link_update: null argument");
+  need_ctx(ctx, U);
+  need_ctx(ctx, P);
+  check_md(prm);
+  need_kind(U, GF_LINK64, "gf_md_link_update: U");
+  need_kind(P, GF_MOM64, "gf_md_link_update: P");
+  need(std::isfinite(eps), "gf_md_link_update: the gauge-field step size must be finite");
+  link_update(ctx, U, P, eps, prm->reunitarize, nullptr, prm->precision != GF_FP64);
   API_END(ctx)
 }
 

@@ -33,9 +33,9 @@ void count_launch();
 
 #define GF_PROF_CAP 4096
 
-// Internal stack precision: fp64 storage with double-float arithmetic (the
-// mixed form's Hamiltonian); never accepted from the C-ABI.
-#define GF_PREC_DF 2
+// Stack precision with fp64 storage and double-float arithmetic: the
+// GF_DFLOAT form, and the Hamiltonian of the mixed form (forward only).
+#define GF_PREC_DF GF_DFLOAT
 
 struct gf_field {
   gf_ctx* ctx;
@@ -63,7 +63,7 @@ struct gf_ctx {
   gf_field* w_link32;     // fp32 12-real shadow of the thin links (mixed form)
   gf_stout* w_stout64;    // stout workspace, fp64
   gf_stout* w_stout32;    // stout workspace, fp32
-  gf_stout* w_stoutdf;    // stout forward for the mixed form's Hamiltonian (double-float)
+  gf_stout* w_stoutdf;    // double-float stack: mixed-form Hamiltonian (forward only) or GF_DFLOAT
   int w_stout_nlev;
   double w_stout_rho[GF_MAX_STOUT];
   // potential of the last configuration an MD call ended on, keyed by a
@@ -91,8 +91,9 @@ struct gf_stout {
   gf_ctx* ctx;
   int nlev;
   double rho[GF_MAX_STOUT];
-  int precision;  // GF_FP64 or GF_FP32
+  int precision;  // GF_FP64, GF_MIXED or GF_PREC_DF
   int store;      // 1: keep C of every level from the forward pass
+  int fwd_only;   // 1: no adjoint buffers (a Hamiltonian-only stack)
   gf_field* lev_in[GF_MAX_STOUT + 1];  // lev_in[0] aliases the thin links
   gf_field* C[GF_MAX_STOUT];
   gf_field* Z;   // dS/dC of the level being pulled back
@@ -149,7 +150,7 @@ double plaquette_sum(gf_ctx* ctx, const gf_field* U, bool df = false);  // sum_x
 void staple_up(gf_ctx* ctx, const gf_field* U, int mu, gf_field* V);  // construct_staple! (mu field slot)
 // P <- keep * P + coef * TA-coefficients(U_mu * S_mu), S = sum of the six
 // staples (dS/dU order); keep = 0 overwrites P without reading it.
-void wilson_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double coef, double keep);
+void wilson_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double coef, double keep, bool df = false);
 
 // ---- link update (gf_update.cu) ----
 // U <- exp(i eps P) U, optional re-unitarisation, optional fp32 shadow copy.

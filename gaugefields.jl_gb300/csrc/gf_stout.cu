@@ -51,13 +51,15 @@ struct Prec<float> {
   }
 };
 
-// fp64 storage, double-float arithmetic: forward only (the mixed form's
-// Hamiltonian smears in this precision)
+// fp64 storage, double-float arithmetic (the GF_DFLOAT form; the mixed
+// form's Hamiltonian smears in this precision)
 template <>
 struct Prec<dfl> {
   typedef LinkSrc<dfl, false> Src;
   typedef double2 LinkElem;
   typedef double2 MatElem;
+  static constexpr int link_kind = GF_LINK64;
+  static constexpr int mat_kind = GF_MAT64;
   static __device__ __forceinline__ void store_link(double2* p, int mu, int s, int V, const mat3<dfl>& m) {
     LinkFull<dfl>::store(p, mu, s, V, m);
   }
@@ -100,7 +102,7 @@ __global__ void __launch_bounds__(128, GF_MINB(R))
 // backward, local part
 // --------------------------------------------------------------------------
 template <typename R, bool TOP>
-__global__ void __launch_bounds__(128, GF_MINB(R))
+__global__ void __launch_bounds__(128, GF_MINB_ADJ(R))
     k_bwd_local(typename Prec<R>::Src U, typename Prec<R>::Src Utop, const typename Prec<R>::MatElem* __restrict__ Dbar,
                 const typename Prec<R>::MatElem* __restrict__ Cst, typename Prec<R>::MatElem* __restrict__ Zout,
                 typename Prec<R>::MatElem* __restrict__ Dpout, Geom g, R rho, R halfbeta) {
@@ -202,7 +204,7 @@ __device__ __forceinline__ void gather_axis(mat3<R>& acc, const typename Prec<R>
 }
 
 template <typename R, bool FORCE>
-__global__ void __launch_bounds__(128, GF_MINB(R))
+__global__ void __launch_bounds__(128, GF_MINB_ADJ(R))
     k_bwd_gather(typename Prec<R>::Src U, const typename Prec<R>::MatElem* __restrict__ Z,
                  const typename Prec<R>::MatElem* __restrict__ Dp, typename Prec<R>::MatElem* __restrict__ Dout,
                  double* __restrict__ P, Geom g, R rho, double coef) {
@@ -223,7 +225,7 @@ __global__ void __launch_bounds__(128, GF_MINB(R))
     ta_coeffs(M, c);
     double* p = P + (size_t)nu * 8 * V + s;
 #pragma unroll
-    for (int a = 0; a < 8; ++a) p[(size_t)a * V] += coef * (double)c[a];
+    for (int a = 0; a < 8; ++a) p[(size_t)a * V] += coef * to_f64(c[a]);
   } else {
     LinkFull<R>::store(Dout, nu, s, V, d);
   }
@@ -239,12 +241,17 @@ static typename Prec<R>::Src src_of(const gf_field* f) {
   return s;
 }
 
+// profiling class of a kernel stage in arithmetic type R
+template <typename R>
+static int kclass(int f32, int f64, int df) {
+  return std::is_same<R, float>::value ? f32 : (std::is_same<R, double>::value ? f64 : df);
+}
+
 template <typename R>
 static void forward_impl(gf_ctx* ctx, gf_stout* st) {
   dim3 grid = stencil_grid(ctx->geom.vol, 128);
   for (int l = 0; l < st->nlev; ++l) {
-    ProfScope prof(ctx, std::is_same<R, float>::value ? GF_K_STOUT_FWD
-                        : (std::is_same<R, double>::value ? GF_K_STOUT_FWD64 : GF_K_STOUT_FWD_DF));
+    ProfScope prof(ctx, kclass<R>(GF_K_STOUT_FWD, GF_K_STOUT_FWD64, GF_K_STOUT_FWD_DF));
     k_stout_fwd<R><<<grid, 128, 0, ctx->stream>>>(
         src_of<R>(st->lev_in[l]), (typename Prec<R>::LinkElem*)st->lev_in[l + 1]->ptr,
         st->store ? (typename Prec<R>::MatElem*)st->C[l]->ptr : nullptr, ctx->geom, (R)st->rho[l]);
@@ -292,7 +299,7 @@ static void backward_impl(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, do
     const ME* Cst = st->store ? (const ME*)st->C[l]->ptr : nullptr;
     const ME* din = (l == st->nlev - 1) ? dbar : (const ME*)st->D[cur]->ptr;
     {
-    ProfScope prof(ctx, sizeof(R) == 8 ? GF_K_BWD_LOCAL64 : GF_K_BWD_LOCAL);
+    ProfScope prof(ctx, kclass<R>(GF_K_BWD_LOCAL, GF_K_BWD_LOCAL64, GF_K_BWD_LOCAL_DF));
     if (top) {
       k_bwd_local<R, true><<<grid, 128, 0, ctx->stream>>>(src_of<R>(st->lev_in[l]), src_of<R>(st->lev_in[l + 1]),
                                                           nullptr, Cst, (ME*)st->Z->ptr, (ME*)st->Dp->ptr, ctx->geom,
@@ -305,7 +312,7 @@ static void backward_impl(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, do
     GF_CHECK_LAUNCH();
     }
     int nxt = cur ^ 1;
-    ProfScope prof(ctx, sizeof(R) == 8 ? GF_K_BWD_GATHER64 : GF_K_BWD_GATHER);
+    ProfScope prof(ctx, kclass<R>(GF_K_BWD_GATHER, GF_K_BWD_GATHER64, GF_K_BWD_GATHER_DF));
     if (l == 0 && P) {
       k_bwd_gather<R, true><<<grid, 128, 0, ctx->stream>>>(src_of<R>(st->lev_in[0]), (const ME*)st->Z->ptr,
                                                            (const ME*)st->Dp->ptr, nullptr, (double*)P->ptr,
@@ -324,12 +331,13 @@ static void backward_impl(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, do
 void stout_backward(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, double beta, gf_field* dSdU, gf_field* P,
                     double eps) {
   if (!st->have_forward) throw gf_error(GF_ESTATE, "stout backward called before forward");
-  if (st->precision == GF_PREC_DF) throw gf_error(GF_EINVAL, "stout backward: forward-only stack");
+  if (st->fwd_only) throw gf_error(GF_EINVAL, "stout backward: forward-only stack");
   if (st->nlev < 1) throw gf_error(GF_EINVAL, "stout backward needs at least one level");
-  int mk = st->precision == GF_FP64 ? GF_MAT64 : GF_MAT32;
+  int mk = st->precision == GF_MIXED ? GF_MAT32 : GF_MAT64;
   if (dSdUbar && dSdUbar->kind != mk) throw gf_error(GF_EINVAL, "stout backward: dS/dUbar kind does not match the stack precision");
   if (!P && (!dSdU || dSdU->kind != mk)) throw gf_error(GF_EINVAL, "stout backward: dS/dU kind does not match the stack precision");
   if (st->precision == GF_FP64) backward_impl<double>(ctx, st, dSdUbar, beta, dSdU, P, eps);
+  else if (st->precision == GF_PREC_DF) backward_impl<dfl>(ctx, st, dSdUbar, beta, dSdU, P, eps);
   else backward_impl<float>(ctx, st, dSdUbar, beta, dSdU, P, eps);
 }
 

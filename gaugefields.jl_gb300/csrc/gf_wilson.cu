@@ -1,5 +1,6 @@
 // Wilson-action kernels: plaquette/action reduction, staples and the fused
-// force + momentum update, for fp64 links and for fp32 12-real links.
+// force + momentum update, for fp64 links (fp64 or double-float arithmetic)
+// and for fp32 12-real links.
 #include "gf_internal.h"
 #include "stencil.cuh"
 
@@ -7,6 +8,7 @@ namespace gf {
 
 typedef LinkSrc<double, false> Src64;
 typedef LinkSrc<float, true> Src32;
+typedef LinkSrc<dfl, false> SrcDF;
 
 // Per-site plaquette sum, one partial per block (calculate_Plaquette,
 // src/AbstractGaugefields.jl:2684-2699, evaluated plaquette by plaquette).
@@ -93,15 +95,20 @@ __global__ void __launch_bounds__(128, GF_MINB(R)) k_force_ta(SRC U, double* __r
 #pragma unroll
   for (int a = 0; a < 8; ++a) {
     double old = (keep != 0.0) ? keep * p[(size_t)a * V] : 0.0;
-    p[(size_t)a * V] = old + coef * (double)c[a];
+    p[(size_t)a * V] = old + coef * to_f64(c[a]);
   }
 }
 
-void wilson_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double coef, double keep) {
+void wilson_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double coef, double keep, bool df) {
   if (P->kind != GF_MOM64) throw gf_error(GF_EINVAL, "force: output must be MOM64");
   dim3 grid = stencil_grid(ctx->geom.vol, 128);
-  ProfScope prof(ctx, GF_K_FORCE);
-  if (U->kind == GF_LINK64) {
+  ProfScope prof(ctx, df ? GF_K_FORCE_DF : GF_K_FORCE);
+  if (df && U->kind == GF_LINK64) {
+    SrcDF src{(const double2*)U->ptr};
+    k_force_ta<dfl><<<grid, 128, 0, ctx->stream>>>(src, (double*)P->ptr, ctx->geom, coef, keep);
+  } else if (df) {
+    throw gf_error(GF_EINVAL, "force: the double-float force needs LINK64 links");
+  } else if (U->kind == GF_LINK64) {
     Src64 src{(const double2*)U->ptr};
     k_force_ta<double><<<grid, 128, 0, ctx->stream>>>(src, (double*)P->ptr, ctx->geom, coef, keep);
   } else if (U->kind == GF_LINK32) {

@@ -98,6 +98,20 @@ struct minblocks<dfl> {
   static constexpr int value = GF_DF_MINB;
 };
 #define GF_MINB(R) (minblocks<R>::value)
+// The double-float adjoint kernels hold twice the fp32 state; at three blocks
+// per SM they spill heavily, so they keep two (255 registers a thread).
+#ifndef GF_DF_ADJ_MINB
+#define GF_DF_ADJ_MINB 2
+#endif
+template <typename R>
+struct minblocks_adj {
+  static constexpr int value = minblocks<R>::value;
+};
+template <>
+struct minblocks_adj<dfl> {
+  static constexpr int value = GF_DF_ADJ_MINB;
+};
+#define GF_MINB_ADJ(R) (minblocks_adj<R>::value)
 
 // Link index of a stencil thread. With GF_INTERLEAVE the grid is 1-D with
 // 4 * ceil(V/bs) blocks and block b handles direction b % 4 of the sites of

@@ -541,7 +541,7 @@ struct dacc {
 };
 
 GF_HD void dacc_add(dacc& a, float xh, float xl, float yh, float yl) {
-  float p = xh * yh;
+  float p = df_mul_rn(xh, yh);  // not fusible: TwoSum below needs fl(xh*yh)
   float pe = fmaf(xh, yh, -p);
   float t = a.s + p;
   float z = t - a.s;

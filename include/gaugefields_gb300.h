@@ -45,6 +45,11 @@ extern "C" {
 /* precision of the force / stout path */
 #define GF_FP64 0  /* plain form: fp64 throughout */
 #define GF_MIXED 1 /* fp32 force and stout (12-real links), fp64 H / updates */
+#define GF_DFLOAT 2 /* force, stout forward/adjoint and link updates in
+                       double-float arithmetic (fp32 pairs, ~48-bit
+                       significand, on the fp32 pipes) on fp64 links; fp64
+                       H, Delta H and Metropolis. No counterpart in the
+                       reference: a third form between GF_FP64 and GF_MIXED */
 
 /* integrators of the MD driver (molecular_dynamics.jl:604-616); GF_OMELYAN is
  * the second-order minimum-norm PQPQP scheme of the reference's custom
@@ -68,7 +73,7 @@ typedef struct gf_md_params {
   double tau;            /* trajectory_length, finite and nonzero */
   int steps;             /* > 0 */
   int integrator;        /* GF_QPQ, GF_PQP or GF_OMELYAN */
-  int precision;         /* GF_FP64 or GF_MIXED */
+  int precision;         /* GF_FP64, GF_MIXED or GF_DFLOAT */
   int nstout;            /* 0 .. GF_MAX_STOUT smearing levels */
   double rho[GF_MAX_STOUT];
   int reunitarize;       /* re-unitarise links after every link update */
@@ -156,9 +161,16 @@ int gf_link_update(gf_ctx* ctx, gf_field* U, const gf_field* P, double eps, int 
 /* md_hamiltonian (molecular_dynamics.jl:494-505): potential (on the smeared
  * links when nstout > 0) + P*P/2, in fp64. */
 int gf_hamiltonian(gf_ctx* ctx, const gf_field* U, const gf_field* P, const gf_md_params* prm, double* out);
+/* update_momenta!(P, U, eps, driver) and update_gaugefields!(U, P, eps,
+ * driver) (molecular_dynamics.jl:539-551, :513-531) with the driver's action,
+ * smearing and precision, as one step of gf_md_trajectory takes them: the
+ * building blocks of custom integrators (md_step! of user types, :593-602).
+ * gf_md_link_update re-unitarises when prm->reunitarize != 0. */
+int gf_md_mom_update(gf_ctx* ctx, gf_field* P, const gf_field* U, double eps, const gf_md_params* prm);
+int gf_md_link_update(gf_ctx* ctx, gf_field* U, const gf_field* P, double eps, const gf_md_params* prm);
 /* md_trajectory!(U, P, driver) (molecular_dynamics.jl:712-730): one QPQ/PQP
  * trajectory. out[0..2] = initial H, final H, Delta H. prm->precision selects
- * the plain fp64 or the mixed form. */
+ * the plain fp64, the mixed or the double-float form. */
 int gf_md_trajectory(gf_ctx* ctx, gf_field* U, gf_field* P, const gf_md_params* prm, double out[3]);
 /* One HMC update of the application loop (docs/src/hmc.md:22-81): momenta
  * refresh (seed, sweep), md_trajectory!, Metropolis test with the uniform
@@ -168,8 +180,9 @@ int gf_hmc_update(gf_ctx* ctx, gf_field* U, gf_field* P, const gf_md_params* prm
 
 /* ---- stout smearing ----------------------------------------------------- */
 /* STOUT_Layer stack (stout_fast.jl:6-121) / CovNeuralnet of nlev plaquette
- * layers with coefficients rho[0..nlev-1]. precision GF_FP64 or GF_MIXED
- * (fp32 12-real links); store != 0 keeps C_mu of every level from the
+ * layers with coefficients rho[0..nlev-1]. precision GF_FP64, GF_MIXED
+ * (fp32 12-real links) or GF_DFLOAT (fp64 links and MAT64 derivatives,
+ * double-float arithmetic); store != 0 keeps C_mu of every level from the
  * forward pass, store == 0 recomputes it in the backward pass. */
 int gf_stout_create(gf_ctx* ctx, int nlev, const double* rho, int precision, int store, gf_stout** out);
 int gf_stout_destroy(gf_stout* st);
@@ -225,8 +238,11 @@ int gf_plaquette_noalloc(const void* links, const int L[4], double* out, void* s
 #define GF_K_BWD_GATHER64 8
 #define GF_K_OTHER 9        /* starts, conversions, kinetic, copies */
 #define GF_K_LINK_UPDATE_DF 10  /* link update in double-float (mixed form) */
-#define GF_K_STOUT_FWD_DF 11    /* stout forward in double-float (mixed-form Hamiltonian) */
-#define GF_K_COUNT 12
+#define GF_K_STOUT_FWD_DF 11    /* stout forward in double-float (Hamiltonian, GF_DFLOAT force) */
+#define GF_K_FORCE_DF 12        /* Wilson staple force in double-float */
+#define GF_K_BWD_LOCAL_DF 13    /* stout adjoint, local part, double-float */
+#define GF_K_BWD_GATHER_DF 14   /* stout adjoint, gather (+ force), double-float */
+#define GF_K_COUNT 15
 /* Enable (on != 0) or disable CUDA-event timing of every kernel launch on the
  * context's stream; enabling clears the accumulators. */
 int gf_prof_enable(gf_ctx* ctx, int on);

@@ -103,6 +103,9 @@ def test_md_driver_with_smearing_params(pkg):
     drv = pkg.md_driver(U, action, steps=20, smearing=net, precision="mixed")
     p = drv.params()
     assert p.nstout == 2 and list(p.rho)[:2] == [0.1, 0.12] and p.precision == 1
+    assert pkg.md_driver(U, action, steps=20, smearing=net, precision="dfloat").params().precision == 2
+    with pytest.raises(ValueError):
+        pkg.md_driver(U, action, steps=20, smearing=net, precision="fp32")
 
 
 def test_api_argument_validation(pkg):
