@@ -65,18 +65,10 @@ __device__ __forceinline__ void mac_aa(mat3<R>& acc, const mat3<R>& a, const mat
 }
 
 // double-float accumulating products as compensated dot products
-__device__ __forceinline__ void mac_nn(mat3<dfl>& acc, const mat3<dfl>& a, const mat3<dfl>& b) {
-  acc = df_matmul<false, false, true>(a, b, &acc);
-}
-__device__ __forceinline__ void mac_na(mat3<dfl>& acc, const mat3<dfl>& a, const mat3<dfl>& b) {
-  acc = df_matmul<false, true, true>(a, b, &acc);
-}
-__device__ __forceinline__ void mac_an(mat3<dfl>& acc, const mat3<dfl>& a, const mat3<dfl>& b) {
-  acc = df_matmul<true, false, true>(a, b, &acc);
-}
-__device__ __forceinline__ void mac_aa(mat3<dfl>& acc, const mat3<dfl>& a, const mat3<dfl>& b) {
-  acc = df_matmul<true, true, true>(a, b, &acc);
-}
+__device__ __forceinline__ void mac_nn(mat3<dfl>& acc, const mat3<dfl>& a, const mat3<dfl>& b) { df_mac<false, false>(acc, a, b); }
+__device__ __forceinline__ void mac_na(mat3<dfl>& acc, const mat3<dfl>& a, const mat3<dfl>& b) { df_mac<false, true>(acc, a, b); }
+__device__ __forceinline__ void mac_an(mat3<dfl>& acc, const mat3<dfl>& a, const mat3<dfl>& b) { df_mac<true, false>(acc, a, b); }
+__device__ __forceinline__ void mac_aa(mat3<dfl>& acc, const mat3<dfl>& a, const mat3<dfl>& b) { df_mac<true, true>(acc, a, b); }
 
 template <typename R, class SRC>
 __device__ __forceinline__ void add_staple_pair(mat3<R>& acc, const SRC& U, const Geom& g, const Site& st, int s,

@@ -554,13 +554,15 @@ GF_HD void dacc_add(dacc& a, float xh, float xl, float yh, float yl) {
 
 GF_HD dfl dacc_get(const dacc& a) { return df_two_sum(a.s, a.c); }
 
-// acc(i,j) (+)= sum_k op(a)_ik op(b)_kj with op = identity or dagger
+// acc(i,j) (+)= sum_k op(a)_ik op(b)_kj with op = identity or dagger.
+// Fully unrolled and inlined: an out-of-line form with rolled entry loops
+// (matrices by value) was 1.3x slower in the stencil kernels, and the forms
+// that indexed the caller's matrices through pointers or dynamic indices came
+// out wrong under nvcc 13.0 -O3 (products of matrices built in registers read
+// stale values).
 template <bool DA, bool DB, bool ACC>
 GF_HD mat3<dfl> df_matmul(const mat3<dfl>& a, const mat3<dfl>& b, const mat3<dfl>* c) {
   mat3<dfl> r;
-  // Keep all three loops unrolled: a rolled row loop (unroll 1) compiled to
-  // wrong staple sums inside the double-float stout kernels, although each
-  // product alone was correct.
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -586,17 +588,18 @@ GF_HD mat3<dfl> df_matmul(const mat3<dfl>& a, const mat3<dfl>& b, const mat3<dfl
   return r;
 }
 
-__device__ __forceinline__ mat3<dfl> mul_nn(const mat3<dfl>& a, const mat3<dfl>& b) {
-  return df_matmul<false, false, false>(a, b, nullptr);
+template <bool DA, bool DB>
+__device__ __forceinline__ mat3<dfl> df_mul(const mat3<dfl>& a, const mat3<dfl>& b) {
+  return df_matmul<DA, DB, false>(a, b, nullptr);
 }
-__device__ __forceinline__ mat3<dfl> mul_na(const mat3<dfl>& a, const mat3<dfl>& b) {
-  return df_matmul<false, true, false>(a, b, nullptr);
+template <bool DA, bool DB>
+__device__ __forceinline__ void df_mac(mat3<dfl>& acc, const mat3<dfl>& a, const mat3<dfl>& b) {
+  acc = df_matmul<DA, DB, true>(a, b, &acc);
 }
-__device__ __forceinline__ mat3<dfl> mul_an(const mat3<dfl>& a, const mat3<dfl>& b) {
-  return df_matmul<true, false, false>(a, b, nullptr);
-}
-__device__ __forceinline__ mat3<dfl> mul_aa(const mat3<dfl>& a, const mat3<dfl>& b) {
-  return df_matmul<true, true, false>(a, b, nullptr);
-}
+
+__device__ __forceinline__ mat3<dfl> mul_nn(const mat3<dfl>& a, const mat3<dfl>& b) { return df_mul<false, false>(a, b); }
+__device__ __forceinline__ mat3<dfl> mul_na(const mat3<dfl>& a, const mat3<dfl>& b) { return df_mul<false, true>(a, b); }
+__device__ __forceinline__ mat3<dfl> mul_an(const mat3<dfl>& a, const mat3<dfl>& b) { return df_mul<true, false>(a, b); }
+__device__ __forceinline__ mat3<dfl> mul_aa(const mat3<dfl>& a, const mat3<dfl>& b) { return df_mul<true, true>(a, b); }
 
 }  // namespace gf
