@@ -185,7 +185,7 @@ def read_traffic(kclass, L):
 # ---------------------------------------------------------------------------
 # this library
 # ---------------------------------------------------------------------------
-def make_setup(pkg, L, precision, seed):
+def make_setup(pkg, L, precision, seed, steps=None):
     U = pkg.gauge_configuration((L,) * 4, start="hot", seed=seed)
     P = pkg.gauge_momenta(U)
     action = pkg.GaugeAction(U)
@@ -193,7 +193,7 @@ def make_setup(pkg, L, precision, seed):
     net = pkg.CovNeuralnet(U)
     for r in RHO:
         pkg.push_(net, pkg.STOUT_Layer("plaquette", r))
-    drv = pkg.md_driver(U, action, steps=NSTEPS, trajectory_length=TAU, smearing=net, precision=precision)
+    drv = pkg.md_driver(U, action, steps=steps or NSTEPS, trajectory_length=TAU, smearing=net, precision=precision)
     return U, P, drv
 
 
@@ -388,17 +388,18 @@ def run_reference(args):
 
 
 def run_precision_mode(args):
-    """Mixed vs plain fp64 from one thermalised configuration: thermalise with
-    `--therm` mixed trajectories from a Haar start (kept unconditionally), then
-    `--steps` trajectories, each from that same configuration with fresh
-    momenta, in both forms. Reports |dH_mixed - dH_fp64|, the agreement of the
-    Metropolis decisions under the same uniform, and the plaquette difference."""
+    """Mixed and double-float vs plain fp64 from one thermalised configuration:
+    thermalise with `--therm` mixed trajectories from a Haar start (kept
+    unconditionally), then `--steps` trajectories, each from that same
+    configuration with fresh momenta, in every form. Reports |dH_form -
+    dH_fp64|, the agreement of the Metropolis decisions under the same
+    uniform, the plaquette difference and each form's seconds per trajectory."""
     import numpy as np
     import torch
     import __graft_entry__ as entry
     pkg = entry.build()
     L = args.lattice
-    U, P, drv = make_setup(pkg, L, "mixed", SEED)
+    U, P, drv = make_setup(pkg, L, "mixed", SEED, args.md_steps)
     t0 = time.perf_counter()
     for t in range(args.therm):
         pkg.gaussian_momenta_(P, seed=SEED + 11, sweep=t)
@@ -407,29 +408,41 @@ def run_precision_mode(args):
     U0 = U.to_host()
     plaq0 = pkg.measure_plaquette(U)
     del U, P, drv
-    forms = {f: make_setup(pkg, L, f, SEED) for f in ("fp64", "mixed")}
+    names = ("fp64", "mixed") + (() if args.no_dfloat else ("dfloat",))
+    forms = {f: make_setup(pkg, L, f, SEED, args.md_steps) for f in names}
     rng = np.random.RandomState(2024)
     rows = []
+    secs = {f: 0.0 for f in names}
     for i in range(args.steps):
         u = rng.uniform()
         r = {}
         for f, (Uf, Pf, df) in forms.items():
             Uf.from_host(U0)
             pkg.gaussian_momenta_(Pf, seed=SEED + 1000, sweep=i)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
             res = pkg.md_trajectory_(Uf, Pf, df)
+            secs[f] += time.perf_counter() - t1
             r[f] = (res.delta_hamiltonian, pkg.measure_plaquette(Uf))
         acc64 = u < np.exp(-r["fp64"][0])
-        accm = u < np.exp(-r["mixed"][0])
-        rows.append({"dH_fp64": r["fp64"][0], "dH_mixed": r["mixed"][0],
-                     "abs_diff": abs(r["mixed"][0] - r["fp64"][0]), "plaq_diff": abs(r["mixed"][1] - r["fp64"][1]),
-                     "same_decision": bool(acc64 == accm)})
-    d = [x["abs_diff"] for x in rows]
-    out = {"mode": "precision", "lattice": [L] * 4, "workload": workload_name(L), "therm": args.therm,
-           "therm_seconds": t_therm, "plaquette_start": plaq0, "trajectories": len(rows),
-           "abs_dH_diff_max": max(d), "abs_dH_diff_median": float(np.median(d)),
-           "same_decision": sum(x["same_decision"] for x in rows),
-           "plaq_diff_max": max(x["plaq_diff"] for x in rows),
-           "dH_fp64_median_abs": float(np.median([abs(x["dH_fp64"]) for x in rows])), "rows": rows}
+        row = {"dH_fp64": r["fp64"][0]}
+        for f in names[1:]:
+            row["dH_" + f] = r[f][0]
+            row["abs_diff_" + f] = abs(r[f][0] - r["fp64"][0])
+            row["plaq_diff_" + f] = abs(r[f][1] - r["fp64"][1])
+            row["same_decision_" + f] = bool(acc64 == (u < np.exp(-r[f][0])))
+        rows.append(row)
+    out = {"mode": "precision", "lattice": [L] * 4, "workload": workload_name(L), "md_steps": args.md_steps or NSTEPS,
+           "therm": args.therm, "therm_seconds": t_therm, "plaquette_start": plaq0, "trajectories": len(rows),
+           "dH_fp64_median_abs": float(np.median([abs(x["dH_fp64"]) for x in rows])),
+           "seconds_per_trajectory": {f: secs[f] / len(rows) for f in names}}
+    for f in names[1:]:
+        d = [x["abs_diff_" + f] for x in rows]
+        out[f] = {"abs_dH_diff_max": max(d), "abs_dH_diff_median": float(np.median(d)),
+                  "within_1e-4": sum(v <= 1e-4 for v in d),
+                  "same_decision": sum(x["same_decision_" + f] for x in rows),
+                  "plaq_diff_max": max(x["plaq_diff_" + f] for x in rows)}
+    out["rows"] = rows
     print(json.dumps(out))
     return 0
 
@@ -603,6 +616,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-dfloat", action="store_true", help="skip the double-float form's line")
+    ap.add_argument("--md-steps", type=int, default=None, help="MD steps per trajectory (default 20)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--therm", type=int, default=10, help="thermalisation trajectories before the Delta H check")
     ap.add_argument("--mode", default="hmc", choices=["hmc", "force", "link", "precision", "wilson", "scale"],

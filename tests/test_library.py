@@ -121,3 +121,28 @@ def test_api_argument_validation(pkg):
         pkg.gradient_flow(None, steps=0)
     with pytest.raises(ValueError):
         pkg.gradient_flow(None, step_size=-0.1)
+
+
+def test_md_params_layout_matches_the_header(pkg, tmp_path):
+    """The ctypes mirror of gf_md_params has the header's size and offsets."""
+    import shutil
+    import subprocess
+    from gaugefields_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    fields = [f for f, _ in _lib.MDParams._fields_]
+    cnames = {"lam": "lambda"}
+    src = tmp_path / "layout.c"
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gaugefields_gb300.h"', "int main(void) {",
+             '  printf("size %zu\\n", sizeof(gf_md_params));']
+    for f in fields:
+        lines.append('  printf("%s %%zu\\n", offsetof(gf_md_params, %s));' % (f, cnames.get(f, f)))
+    lines += ["  return 0;", "}"]
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = dict(l.split() for l in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n") if l)
+    assert int(out["size"]) == ctypes.sizeof(_lib.MDParams)
+    for f in fields:
+        assert int(out[f]) == getattr(_lib.MDParams, f).offset, f
