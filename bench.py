@@ -585,12 +585,13 @@ def run_scale_mode(args):
 
 def run_kernel_mode(args):
     """Small single-family cases for profiler captures: `force` repeats the
-    mixed stout force (gf_stout_mom_update), `link` the fp64 link update."""
+    stout force of the workload (update_momenta_), `link` the link update
+    (update_gaugefields_), both in the form `--precision` names."""
     import torch
     import __graft_entry__ as entry
     pkg = entry.build()
     L = args.lattice
-    U, P, drv = make_setup(pkg, L, "mixed", SEED)
+    U, P, drv = make_setup(pkg, L, args.precision, SEED)
     pkg.gaussian_momenta_(P, seed=SEED)
     calls = []
     for k in range(args.warmup + args.steps):
@@ -602,7 +603,8 @@ def run_kernel_mode(args):
             pkg.update_gaugefields_(U, P, 0.01, drv)
         U.ctx.sync()
         calls.append(time.perf_counter() - t0)
-    print(json.dumps({"mode": args.mode, "lattice": [L] * 4, "ms_per_call": 1e3 * min(calls[args.warmup:])}))
+    print(json.dumps({"mode": args.mode, "precision": args.precision, "lattice": [L] * 4,
+                      "ms_per_call": 1e3 * min(calls[args.warmup:])}))
     return 0
 
 
@@ -617,6 +619,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-dfloat", action="store_true", help="skip the double-float form's line")
     ap.add_argument("--md-steps", type=int, default=None, help="MD steps per trajectory (default 20)")
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed", "dfloat"],
+                    help="form of the force/link modes")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--therm", type=int, default=10, help="thermalisation trajectories before the Delta H check")
     ap.add_argument("--mode", default="hmc", choices=["hmc", "force", "link", "precision", "wilson", "scale"],

@@ -116,39 +116,55 @@ using dfns::df_fast_two_sum;
 using dfns::df_two_prod;
 using dfns::df_mul_rn;
 
-// Split an fp64 value into hi + lo fp32 parts with integer operations only:
-// hi keeps the sign, exponent and leading 23 fraction bits (truncated), lo the
-// remaining 29 bits rounded to fp32, so hi + lo equals the double to 2^-53
-// relative. Zero maps to zero; magnitudes between 2^-70 and 2^100 (all link,
-// momentum and staple entries) take the integer path, others (never met on
-// this path) an fp64 conversion.
+// Split an fp64 value into hi + lo fp32 parts without fp64 instructions (on
+// GB300 one fp64 warp instruction occupies the fp64 pipe for as long as ~64
+// fp32 ones, and these conversions run on every load of a double-float
+// kernel): hi keeps the sign, exponent and leading 23 fraction bits
+// (truncated), lo the remaining 29 bits rounded to fp32, so hi + lo equals the
+// double to 2^-48 relative, the precision of double-float arithmetic. The
+// 29-bit remainder becomes a float through two exact 2^23-offset
+// constructions and one fused multiply-add (no integer conversion
+// instruction). Magnitudes in [2^-74, 2^128) take this path; smaller ones
+// flush to a signed zero (far below 2^-48 of every value they meet on this
+// path; keeping hi alone for them measured 5-12% slower in every
+// double-float kernel), larger ones and infinities give a signed infinity and
+// NaN a NaN.
 __device__ __forceinline__ dfl df_from_double(double d) {
-  unsigned long long b = (unsigned long long)__double_as_longlong(d);
-  if ((b << 1) == 0ull) return dfl(0.f, 0.f);
-  unsigned int sign = (unsigned int)(b >> 63);
-  int e = (int)((b >> 52) & 0x7FF);
-  if (e < 1023 - 70 || e > 1023 + 100) return dfl((float)d, 0.f);
-  unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
-  unsigned int hbits = (sign << 31) | ((unsigned int)(e - 1023 + 127) << 23) | (unsigned int)(mant >> 29);
-  float hi = __int_as_float((int)hbits);
-  unsigned int r = (unsigned int)(mant & 0x1FFFFFFFull);
-  // lo = r * 2^(e - 1023 - 52), built from the exponent bits of the scale
-  float scale = __int_as_float((int)((unsigned int)(e - 1023 - 52 + 127) << 23));
-  float lo = __uint2float_rn(r) * scale;
-  return dfl(hi, sign ? -lo : lo);
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned int w1 = (unsigned int)(b >> 32), w0 = (unsigned int)b;
+  const unsigned int sign = w1 & 0x80000000u;
+  const int e = (int)((w1 >> 20) & 0x7FFu);
+  const unsigned int m23 = ((w1 & 0xFFFFFu) << 3) | (w0 >> 29);
+  const unsigned int r = w0 & 0x1FFFFFFFu;
+  const float two23 = 8388608.0f;
+  const float rl = __uint_as_float(0x4B000000u | (r & 0x7FFFFFu)) - two23;  // exact
+  const float rh = __uint_as_float(0x4B000000u | (r >> 23)) - two23;        // exact
+  const float rv = fmaf(rh, two23, rl);                                      // r rounded to fp32
+  // lo = r * 2^(e - 1023 - 52): the scale's exponent field is e - 948
+  const float scale = __uint_as_float((unsigned int)(e - 948) << 23);
+  float hi = __uint_as_float(sign | ((unsigned int)(e - 896) << 23) | m23);
+  float lo = __uint_as_float(__float_as_uint(rv * scale) ^ sign);
+  if (e < 949) {
+    hi = __uint_as_float(sign);
+    lo = 0.f;
+  } else if (e > 1150) {
+    const bool nan = e == 0x7FF && (m23 | r) != 0u;
+    hi = __uint_as_float(sign | 0x7F800000u | (nan ? 0x400000u : 0u));
+    lo = 0.f;
+  }
+  return dfl(hi, lo);
 }
 
-// fp32 -> fp64 widening with integer operations. Zero and subnormal parts
-// (only ever the lo part of a value below 2^-100) map to zero; infinities and
-// NaN take the fp64 conversion so that they propagate.
+// fp32 -> fp64 widening with integer operations only. Zero and subnormal
+// parts (only ever the lo part of a value below 2^-100) map to a signed zero;
+// infinities and NaN keep their class.
 __device__ __forceinline__ double widen_f32(float f) {
-  unsigned int b = (unsigned int)__float_as_int(f);
-  unsigned int e = (b >> 23) & 0xFFu;
-  if (e == 0u) return 0.0;
-  if (e == 0xFFu) return (double)f;
-  unsigned long long d = ((unsigned long long)(b >> 31) << 63) | ((unsigned long long)(e - 127u + 1023u) << 52) |
-                         ((unsigned long long)(b & 0x7FFFFFu) << 29);
-  return __longlong_as_double((long long)d);
+  const unsigned int b = __float_as_uint(f);
+  const unsigned int e = (b >> 23) & 0xFFu;
+  const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
+  const unsigned long long ex = e == 0u ? 0ull : (e == 0xFFu ? 0x7FFull : (unsigned long long)(e + 896u));
+  const unsigned long long man = e == 0u ? 0ull : (unsigned long long)(b & 0x7FFFFFu) << 29;
+  return __longlong_as_double((long long)(sign | (ex << 52) | man));
 }
 
 // hi + lo as fp64: two integer widenings and one fp64 add

@@ -232,6 +232,113 @@ __global__ void __launch_bounds__(128, GF_MINB_ADJ(R))
 }
 
 // --------------------------------------------------------------------------
+// The double-float gather as a loop over its ten products per axis. Inlined,
+// the ten double-float products of gather_axis (about 2,500 instructions
+// each) overflow the instruction cache and the kernel stalls on instruction
+// fetch. Here one product sits in the body of a run-time loop over a table of
+// operations; the two intermediate matrices t and acc live in per-thread
+// shared-memory slots, the other operands come from the link and Z fields.
+// --------------------------------------------------------------------------
+struct GatherOp {
+  // operand sources: 0 link field U, 1 field Z, 2 slot t; dir 0 = nu, 1 = kappa;
+  // site 0 x, 1 x+nu, 2 x+kappa, 3 x-kappa, 4 x-kappa+nu
+  unsigned char a_src, a_dir, a_site, a_dag, b_src, b_dir, b_site, b_dag, out_acc, accumulate;
+};
+// The terms (a)..(f) of gather_axis in the same factored order.
+__constant__ GatherOp c_gather_ops[10] = {
+    {0, 0, 2, 1, 1, 1, 0, 0, 0, 0},  // t  = U_nu(x+k)^dag Z_k(x)
+    {1, 0, 2, 0, 0, 1, 0, 1, 0, 1},  // t += Z_nu(x+k) U_k(x)^dag
+    {0, 1, 1, 0, 2, 0, 0, 0, 1, 1},  // acc += U_k(x+nu) t
+    {0, 1, 0, 0, 0, 0, 2, 0, 0, 0},  // t  = U_k(x) U_nu(x+k)
+    {1, 1, 1, 1, 2, 0, 0, 1, 1, 1},  // acc += Z_k(x+nu)^dag t^dag
+    {0, 0, 3, 0, 0, 1, 4, 0, 0, 0},  // t  = U_nu(x-k) U_k(x-k+nu)
+    {2, 0, 0, 1, 1, 1, 3, 1, 1, 1},  // acc += t^dag Z_k(x-k)^dag
+    {1, 1, 4, 0, 0, 0, 3, 1, 0, 0},  // t  = Z_k(x-k+nu) U_nu(x-k)^dag
+    {0, 1, 4, 1, 1, 0, 3, 0, 0, 1},  // t += U_k(x-k+nu)^dag Z_nu(x-k)
+    {2, 0, 0, 0, 0, 1, 3, 0, 1, 1},  // acc += t U_k(x-k)
+};
+
+// slot `slot` of this thread: 36 floats, element-major so that a warp's
+// accesses fall in consecutive banks
+__device__ __forceinline__ mat3<dfl> slot_load(const float* sm, int slot, int tid) {
+  mat3<dfl> m;
+#pragma unroll
+  for (int e = 0; e < 9; ++e) {
+    const float* q = sm + (slot * 36 + 4 * e) * 128 + tid;
+    m.e[e / 3][e % 3] = mk(dfl(q[0], q[128]), dfl(q[256], q[384]));
+  }
+  return m;
+}
+__device__ __forceinline__ void slot_store(float* sm, int slot, int tid, const mat3<dfl>& m) {
+#pragma unroll
+  for (int e = 0; e < 9; ++e) {
+    float* q = sm + (slot * 36 + 4 * e) * 128 + tid;
+    const cplx<dfl> v = m.e[e / 3][e % 3];
+    q[0] = v.re.hi;
+    q[128] = v.re.lo;
+    q[256] = v.im.hi;
+    q[384] = v.im.lo;
+  }
+}
+
+template <bool FORCE>
+__global__ void __launch_bounds__(128, GF_MINB_ADJ(dfl))
+    k_bwd_gather_df(const double2* __restrict__ U, const double2* __restrict__ Z, const double2* __restrict__ Dp,
+                    double2* __restrict__ Dout, double* __restrict__ P, Geom g, dfl rho, double coef) {
+  __shared__ float sm[2 * 36 * 128];
+  const int tid = threadIdx.x;
+  int s, nu;
+  link_of_thread(s, nu);
+  const bool live = s < g.vol;  // every thread takes part in the loop; only live ones touch memory
+  const int V = g.vol;
+  const int sc = live ? s : 0;
+  Site st = site_of(g, sc);
+  slot_store(sm, 1, tid, zero3<dfl>());
+#pragma unroll 1
+  for (int k = 1; k < 4; ++k) {
+    const int K = (nu + k) & 3;
+    const int xpn = nbr_rt(g, st, nu, +1), xpk = nbr_rt(g, st, K, +1), xmk = nbr_rt(g, st, K, -1);
+    const int xmk_pn = nbr2_rt(g, st, K, -1, nu, +1);
+#pragma unroll 1
+    for (int q = 0; q < 10; ++q) {
+      const GatherOp op = c_gather_ops[q];
+      mat3<dfl> A, B;
+      {
+        const int site = op.a_site == 0 ? sc : op.a_site == 1 ? xpn : op.a_site == 2 ? xpk : op.a_site == 3 ? xmk : xmk_pn;
+        if (op.a_src == 2) A = slot_load(sm, 0, tid);
+        else A = LinkFull<dfl>::load(op.a_src == 0 ? U : Z, op.a_dir ? K : nu, site, V);
+        if (op.a_dag) A = dag(A);
+      }
+      {
+        const int site = op.b_site == 0 ? sc : op.b_site == 1 ? xpn : op.b_site == 2 ? xpk : op.b_site == 3 ? xmk : xmk_pn;
+        if (op.b_src == 2) B = slot_load(sm, 0, tid);
+        else B = LinkFull<dfl>::load(op.b_src == 0 ? U : Z, op.b_dir ? K : nu, site, V);
+        if (op.b_dag) B = dag(B);
+      }
+      const mat3<dfl> C = op.accumulate ? slot_load(sm, op.out_acc, tid) : zero3<dfl>();
+      slot_store(sm, op.out_acc, tid, df_matmul<false, false, true>(A, B, &C));
+    }
+  }
+  if (!live) return;
+  mat3<dfl> d = LinkFull<dfl>::load(Dp, nu, s, V);
+  axpy_to(d, rho, slot_load(sm, 1, tid));
+  if (FORCE) {
+    const mat3<dfl> M = mul_nn(LinkFull<dfl>::load(U, nu, s, V), d);
+    dfl c[8];
+    ta_coeffs(M, c);
+    double* p = P + (size_t)nu * 8 * V + s;
+#pragma unroll
+    for (int a = 0; a < 8; ++a) p[(size_t)a * V] += coef * to_f64(c[a]);
+  } else {
+    LinkFull<dfl>::store(Dout, nu, s, V, d);
+  }
+}
+
+#ifndef GF_DF_GATHER_LOOP
+#define GF_DF_GATHER_LOOP 1
+#endif
+
+// --------------------------------------------------------------------------
 // host drivers
 // --------------------------------------------------------------------------
 template <typename R>
@@ -313,6 +420,22 @@ static void backward_impl(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, do
     }
     int nxt = cur ^ 1;
     ProfScope prof(ctx, kclass<R>(GF_K_BWD_GATHER, GF_K_BWD_GATHER64, GF_K_BWD_GATHER_DF));
+    if constexpr (GF_DF_GATHER_LOOP && std::is_same<R, dfl>::value) {
+      const double2* u = (const double2*)st->lev_in[l]->ptr;
+      if (l == 0 && P) {
+        k_bwd_gather_df<true><<<grid, 128, 0, ctx->stream>>>(u, (const double2*)st->Z->ptr, (const double2*)st->Dp->ptr,
+                                                             nullptr, (double*)P->ptr, ctx->geom, (R)st->rho[0],
+                                                             -eps / 3.0);
+      } else {
+        double2* out = (l == 0) ? (double2*)dSdU->ptr : (double2*)st->D[nxt]->ptr;
+        k_bwd_gather_df<false><<<grid, 128, 0, ctx->stream>>>(u, (const double2*)st->Z->ptr,
+                                                              (const double2*)st->Dp->ptr, out, nullptr, ctx->geom,
+                                                              (R)st->rho[l], 0.0);
+      }
+      GF_CHECK_LAUNCH();
+      cur = nxt;
+      continue;
+    }
     if (l == 0 && P) {
       k_bwd_gather<R, true><<<grid, 128, 0, ctx->stream>>>(src_of<R>(st->lev_in[0]), (const ME*)st->Z->ptr,
                                                            (const ME*)st->Dp->ptr, nullptr, (double*)P->ptr,
