@@ -232,34 +232,24 @@ __global__ void __launch_bounds__(128, GF_MINB_ADJ(R))
 }
 
 // --------------------------------------------------------------------------
-// The double-float gather as a loop over its ten products per axis. Inlined,
-// the ten double-float products of gather_axis (about 2,500 instructions
-// each) overflow the instruction cache and the kernel stalls on instruction
-// fetch. Here one product sits in the body of a run-time loop over a table of
-// operations; the two intermediate matrices t and acc live in per-thread
-// shared-memory slots, the other operands come from the link and Z fields.
+// Double-float kernels as loops over tables of products. Inlined, every
+// double-float 3x3 product is about 2,500 instructions; the stout kernels hold
+// 14-30 of them, overflow the instruction cache and stall on instruction
+// fetch (ncu). Here one product sits in the body of a run-time loop over a
+// table of operations. Each operand is a link of one of two fields (at one of
+// up to five sites, in one of two directions) or a per-thread slot in shared
+// memory, optionally daggered; the result goes to a slot, optionally added
+// to it. Out-of-line forms of the product were slower (argument passing) or
+// miscompiled (pointers into the caller's registers), which this avoids.
 // --------------------------------------------------------------------------
-struct GatherOp {
-  // operand sources: 0 link field U, 1 field Z, 2 slot t; dir 0 = nu, 1 = kappa;
-  // site 0 x, 1 x+nu, 2 x+kappa, 3 x-kappa, 4 x-kappa+nu
-  unsigned char a_src, a_dir, a_site, a_dag, b_src, b_dir, b_site, b_dag, out_acc, accumulate;
-};
-// The terms (a)..(f) of gather_axis in the same factored order.
-__constant__ GatherOp c_gather_ops[10] = {
-    {0, 0, 2, 1, 1, 1, 0, 0, 0, 0},  // t  = U_nu(x+k)^dag Z_k(x)
-    {1, 0, 2, 0, 0, 1, 0, 1, 0, 1},  // t += Z_nu(x+k) U_k(x)^dag
-    {0, 1, 1, 0, 2, 0, 0, 0, 1, 1},  // acc += U_k(x+nu) t
-    {0, 1, 0, 0, 0, 0, 2, 0, 0, 0},  // t  = U_k(x) U_nu(x+k)
-    {1, 1, 1, 1, 2, 0, 0, 1, 1, 1},  // acc += Z_k(x+nu)^dag t^dag
-    {0, 0, 3, 0, 0, 1, 4, 0, 0, 0},  // t  = U_nu(x-k) U_k(x-k+nu)
-    {2, 0, 0, 1, 1, 1, 3, 1, 1, 1},  // acc += t^dag Z_k(x-k)^dag
-    {1, 1, 4, 0, 0, 0, 3, 1, 0, 0},  // t  = Z_k(x-k+nu) U_nu(x-k)^dag
-    {0, 1, 4, 1, 1, 0, 3, 0, 0, 1},  // t += U_k(x-k+nu)^dag Z_nu(x-k)
-    {2, 0, 0, 0, 0, 1, 3, 0, 1, 1},  // acc += t U_k(x-k)
+struct DfOp {
+  // src: 0 field F0, 1 field F1, 2 + k slot k; dir: 0 the kernel's link
+  // direction, 1 the loop axis; site: index into the kernel's five sites
+  unsigned char a_src, a_dir, a_site, a_dag, b_src, b_dir, b_site, b_dag, out, accumulate;
 };
 
 // slot `slot` of this thread: 36 floats, element-major so that a warp's
-// accesses fall in consecutive banks
+// accesses fall in consecutive banks (blocks of 128 threads)
 __device__ __forceinline__ mat3<dfl> slot_load(const float* sm, int slot, int tid) {
   mat3<dfl> m;
 #pragma unroll
@@ -281,6 +271,45 @@ __device__ __forceinline__ void slot_store(float* sm, int slot, int tid, const m
   }
 }
 
+struct DfSites {
+  int x[5];
+};
+__device__ __forceinline__ int pick_site(const DfSites& st, int i) {
+  return i == 0 ? st.x[0] : i == 1 ? st.x[1] : i == 2 ? st.x[2] : i == 3 ? st.x[3] : st.x[4];
+}
+__device__ __forceinline__ mat3<dfl> df_operand(int src, int dir, int site, int dagger, const float* sm, int tid,
+                                                const double2* F0, const double2* F1, int V, int d0, int d1,
+                                                const DfSites& st) {
+  mat3<dfl> m;
+  if (src >= 2) m = slot_load(sm, src - 2, tid);
+  else m = LinkFull<dfl>::load(src == 0 ? F0 : F1, dir ? d1 : d0, pick_site(st, site), V);
+  if (dagger) m = dag(m);
+  return m;
+}
+__device__ __forceinline__ void df_exec(const DfOp op, float* sm, int tid, const double2* F0, const double2* F1,
+                                        int V, int d0, int d1, const DfSites& st) {
+  const mat3<dfl> A = df_operand(op.a_src, op.a_dir, op.a_site, op.a_dag, sm, tid, F0, F1, V, d0, d1, st);
+  const mat3<dfl> B = df_operand(op.b_src, op.b_dir, op.b_site, op.b_dag, sm, tid, F0, F1, V, d0, d1, st);
+  const mat3<dfl> C = op.accumulate ? slot_load(sm, op.out, tid) : zero3<dfl>();
+  slot_store(sm, op.out, tid, df_matmul<false, false, true>(A, B, &C));
+}
+
+// The gather: F0 = U, F1 = Z, d0 = nu, d1 = kappa; sites x, x+nu, x+kappa,
+// x-kappa, x-kappa+nu; slot 0 = t, slot 1 = acc. The terms (a)..(f) of
+// gather_axis in the same factored order.
+__constant__ DfOp c_gather_ops[10] = {
+    {0, 0, 2, 1, 1, 1, 0, 0, 0, 0},  // t  = U_nu(x+k)^dag Z_k(x)
+    {1, 0, 2, 0, 0, 1, 0, 1, 0, 1},  // t += Z_nu(x+k) U_k(x)^dag
+    {0, 1, 1, 0, 2, 0, 0, 0, 1, 1},  // acc += U_k(x+nu) t
+    {0, 1, 0, 0, 0, 0, 2, 0, 0, 0},  // t  = U_k(x) U_nu(x+k)
+    {1, 1, 1, 1, 2, 0, 0, 1, 1, 1},  // acc += Z_k(x+nu)^dag t^dag
+    {0, 0, 3, 0, 0, 1, 4, 0, 0, 0},  // t  = U_nu(x-k) U_k(x-k+nu)
+    {2, 0, 0, 1, 1, 1, 3, 1, 1, 1},  // acc += t^dag Z_k(x-k)^dag
+    {1, 1, 4, 0, 0, 0, 3, 1, 0, 0},  // t  = Z_k(x-k+nu) U_nu(x-k)^dag
+    {0, 1, 4, 1, 1, 0, 3, 0, 0, 1},  // t += U_k(x-k+nu)^dag Z_nu(x-k)
+    {2, 0, 0, 0, 0, 1, 3, 0, 1, 1},  // acc += t U_k(x-k)
+};
+
 template <bool FORCE>
 __global__ void __launch_bounds__(128, GF_MINB_ADJ(dfl))
     k_bwd_gather_df(const double2* __restrict__ U, const double2* __restrict__ Z, const double2* __restrict__ Dp,
@@ -289,35 +318,22 @@ __global__ void __launch_bounds__(128, GF_MINB_ADJ(dfl))
   const int tid = threadIdx.x;
   int s, nu;
   link_of_thread(s, nu);
-  const bool live = s < g.vol;  // every thread takes part in the loop; only live ones touch memory
+  const bool live = s < g.vol;  // every thread runs the loop; only live ones write global memory
   const int V = g.vol;
   const int sc = live ? s : 0;
-  Site st = site_of(g, sc);
+  const Site st = site_of(g, sc);
   slot_store(sm, 1, tid, zero3<dfl>());
+  DfSites ss;
+  ss.x[0] = sc;
+  ss.x[1] = nbr_rt(g, st, nu, +1);
 #pragma unroll 1
   for (int k = 1; k < 4; ++k) {
     const int K = (nu + k) & 3;
-    const int xpn = nbr_rt(g, st, nu, +1), xpk = nbr_rt(g, st, K, +1), xmk = nbr_rt(g, st, K, -1);
-    const int xmk_pn = nbr2_rt(g, st, K, -1, nu, +1);
+    ss.x[2] = nbr_rt(g, st, K, +1);
+    ss.x[3] = nbr_rt(g, st, K, -1);
+    ss.x[4] = nbr2_rt(g, st, K, -1, nu, +1);
 #pragma unroll 1
-    for (int q = 0; q < 10; ++q) {
-      const GatherOp op = c_gather_ops[q];
-      mat3<dfl> A, B;
-      {
-        const int site = op.a_site == 0 ? sc : op.a_site == 1 ? xpn : op.a_site == 2 ? xpk : op.a_site == 3 ? xmk : xmk_pn;
-        if (op.a_src == 2) A = slot_load(sm, 0, tid);
-        else A = LinkFull<dfl>::load(op.a_src == 0 ? U : Z, op.a_dir ? K : nu, site, V);
-        if (op.a_dag) A = dag(A);
-      }
-      {
-        const int site = op.b_site == 0 ? sc : op.b_site == 1 ? xpn : op.b_site == 2 ? xpk : op.b_site == 3 ? xmk : xmk_pn;
-        if (op.b_src == 2) B = slot_load(sm, 0, tid);
-        else B = LinkFull<dfl>::load(op.b_src == 0 ? U : Z, op.b_dir ? K : nu, site, V);
-        if (op.b_dag) B = dag(B);
-      }
-      const mat3<dfl> C = op.accumulate ? slot_load(sm, op.out_acc, tid) : zero3<dfl>();
-      slot_store(sm, op.out_acc, tid, df_matmul<false, false, true>(A, B, &C));
-    }
+    for (int q = 0; q < 10; ++q) df_exec(c_gather_ops[q], sm, tid, U, Z, V, nu, K, ss);
   }
   if (!live) return;
   mat3<dfl> d = LinkFull<dfl>::load(Dp, nu, s, V);
@@ -334,8 +350,58 @@ __global__ void __launch_bounds__(128, GF_MINB_ADJ(dfl))
   }
 }
 
+// The stout forward: F0 = U, d0 = mu, d1 = nu; sites x, x+mu, x+nu,
+// x+mu-nu, x-nu; slot 0 = t, slot 1 = acc. Ops 0-3 (per nu) build S_mu in
+// dS/dU order as add_staple_pair does; op 4 forms U S; op 5 e^Q U.
+__constant__ DfOp c_stout_ops[6] = {
+    {0, 1, 1, 0, 0, 0, 2, 1, 0, 0},  // t  = U_nu(x+mu) U_mu(x+nu)^dag
+    {2, 0, 0, 0, 0, 1, 0, 1, 1, 1},  // acc += t U_nu(x)^dag
+    {0, 1, 3, 1, 0, 0, 4, 1, 0, 0},  // t  = U_nu(x+mu-nu)^dag U_mu(x-nu)^dag
+    {2, 0, 0, 0, 0, 1, 4, 0, 1, 1},  // acc += t U_nu(x-nu)
+    {0, 0, 0, 0, 3, 0, 0, 0, 0, 0},  // t  = U_mu(x) S
+    {2, 0, 0, 0, 0, 0, 0, 0, 1, 0},  // acc = e^Q U_mu(x)   (slot 0 holds e^Q by then)
+};
+
+__global__ void __launch_bounds__(128, GF_MINB(dfl))
+    k_stout_fwd_df(const double2* __restrict__ U, double2* __restrict__ Uout, double2* __restrict__ Cout, Geom g,
+                   dfl rho) {
+  __shared__ float sm[2 * 36 * 128];
+  const int tid = threadIdx.x;
+  int s, mu;
+  link_of_thread(s, mu);
+  const bool live = s < g.vol;
+  const int V = g.vol;
+  const int sc = live ? s : 0;
+  const Site st = site_of(g, sc);
+  slot_store(sm, 1, tid, zero3<dfl>());
+  DfSites ss;
+  ss.x[0] = sc;
+  ss.x[1] = nbr_rt(g, st, mu, +1);
+  int nu = 0;
+#pragma unroll 1
+  for (int q = 0; q < 14; ++q) {
+    if (q < 12 && (q & 3) == 0) {
+      nu = (mu + 1 + (q >> 2)) & 3;
+      ss.x[2] = nbr_rt(g, st, nu, +1);
+      ss.x[3] = nbr2_rt(g, st, mu, +1, nu, -1);
+      ss.x[4] = nbr_rt(g, st, nu, -1);
+    }
+    if (q == 13) {
+      // Q = TA(rho S^dag U^dag) = -rho TA(U S): exp(Q) = exp(i Qh), Qh = i rho TA(U S)
+      const mat3<dfl> qh = times_i(rho, ta_proj(slot_load(sm, 0, tid)));
+      slot_store(sm, 0, tid, expiq(qh));
+      if (Cout && live) LinkFull<dfl>::store(Cout, mu, s, V, scale(rho, dag(slot_load(sm, 1, tid))));
+    }
+    df_exec(c_stout_ops[q < 12 ? (q & 3) : q - 8], sm, tid, U, U, V, mu, nu, ss);
+  }
+  if (live) LinkFull<dfl>::store(Uout, mu, s, V, slot_load(sm, 1, tid));
+}
+
 #ifndef GF_DF_GATHER_LOOP
 #define GF_DF_GATHER_LOOP 1
+#endif
+#ifndef GF_DF_FWD_LOOP
+#define GF_DF_FWD_LOOP 1
 #endif
 
 // --------------------------------------------------------------------------
@@ -359,6 +425,14 @@ static void forward_impl(gf_ctx* ctx, gf_stout* st) {
   dim3 grid = stencil_grid(ctx->geom.vol, 128);
   for (int l = 0; l < st->nlev; ++l) {
     ProfScope prof(ctx, kclass<R>(GF_K_STOUT_FWD, GF_K_STOUT_FWD64, GF_K_STOUT_FWD_DF));
+    if constexpr (GF_DF_FWD_LOOP && std::is_same<R, dfl>::value) {
+      k_stout_fwd_df<<<grid, 128, 0, ctx->stream>>>((const double2*)st->lev_in[l]->ptr,
+                                                    (double2*)st->lev_in[l + 1]->ptr,
+                                                    st->store ? (double2*)st->C[l]->ptr : nullptr, ctx->geom,
+                                                    (R)st->rho[l]);
+      GF_CHECK_LAUNCH();
+      continue;
+    }
     k_stout_fwd<R><<<grid, 128, 0, ctx->stream>>>(
         src_of<R>(st->lev_in[l]), (typename Prec<R>::LinkElem*)st->lev_in[l + 1]->ptr,
         st->store ? (typename Prec<R>::MatElem*)st->C[l]->ptr : nullptr, ctx->geom, (R)st->rho[l]);
