@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(128, GF_MINB_ADJ(R))
 // miscompiled (pointers into the caller's registers), which this avoids.
 // --------------------------------------------------------------------------
 struct DfOp {
-  // src: 0 field F0, 1 field F1, 2 + k slot k; dir: 0 the kernel's link
+  // src: 0, 1, 2 fields F0, F1, F2, 3 + k slot k; dir: 0 the kernel's link
   // direction, 1 the loop axis; site: index into the kernel's five sites
   unsigned char a_src, a_dir, a_site, a_dag, b_src, b_dir, b_site, b_dag, out, accumulate;
 };
@@ -277,19 +277,21 @@ struct DfSites {
 __device__ __forceinline__ int pick_site(const DfSites& st, int i) {
   return i == 0 ? st.x[0] : i == 1 ? st.x[1] : i == 2 ? st.x[2] : i == 3 ? st.x[3] : st.x[4];
 }
+struct DfFields {
+  const double2* f[3];
+};
 __device__ __forceinline__ mat3<dfl> df_operand(int src, int dir, int site, int dagger, const float* sm, int tid,
-                                                const double2* F0, const double2* F1, int V, int d0, int d1,
-                                                const DfSites& st) {
+                                                const DfFields& F, int V, int d0, int d1, const DfSites& st) {
   mat3<dfl> m;
-  if (src >= 2) m = slot_load(sm, src - 2, tid);
-  else m = LinkFull<dfl>::load(src == 0 ? F0 : F1, dir ? d1 : d0, pick_site(st, site), V);
+  if (src >= 3) m = slot_load(sm, src - 3, tid);
+  else m = LinkFull<dfl>::load(src == 0 ? F.f[0] : src == 1 ? F.f[1] : F.f[2], dir ? d1 : d0, pick_site(st, site), V);
   if (dagger) m = dag(m);
   return m;
 }
-__device__ __forceinline__ void df_exec(const DfOp op, float* sm, int tid, const double2* F0, const double2* F1,
-                                        int V, int d0, int d1, const DfSites& st) {
-  const mat3<dfl> A = df_operand(op.a_src, op.a_dir, op.a_site, op.a_dag, sm, tid, F0, F1, V, d0, d1, st);
-  const mat3<dfl> B = df_operand(op.b_src, op.b_dir, op.b_site, op.b_dag, sm, tid, F0, F1, V, d0, d1, st);
+__device__ __forceinline__ void df_exec(const DfOp op, float* sm, int tid, const DfFields& F, int V, int d0, int d1,
+                                        const DfSites& st) {
+  const mat3<dfl> A = df_operand(op.a_src, op.a_dir, op.a_site, op.a_dag, sm, tid, F, V, d0, d1, st);
+  const mat3<dfl> B = df_operand(op.b_src, op.b_dir, op.b_site, op.b_dag, sm, tid, F, V, d0, d1, st);
   const mat3<dfl> C = op.accumulate ? slot_load(sm, op.out, tid) : zero3<dfl>();
   slot_store(sm, op.out, tid, df_matmul<false, false, true>(A, B, &C));
 }
@@ -300,14 +302,14 @@ __device__ __forceinline__ void df_exec(const DfOp op, float* sm, int tid, const
 __constant__ DfOp c_gather_ops[10] = {
     {0, 0, 2, 1, 1, 1, 0, 0, 0, 0},  // t  = U_nu(x+k)^dag Z_k(x)
     {1, 0, 2, 0, 0, 1, 0, 1, 0, 1},  // t += Z_nu(x+k) U_k(x)^dag
-    {0, 1, 1, 0, 2, 0, 0, 0, 1, 1},  // acc += U_k(x+nu) t
+    {0, 1, 1, 0, 3, 0, 0, 0, 1, 1},  // acc += U_k(x+nu) t
     {0, 1, 0, 0, 0, 0, 2, 0, 0, 0},  // t  = U_k(x) U_nu(x+k)
-    {1, 1, 1, 1, 2, 0, 0, 1, 1, 1},  // acc += Z_k(x+nu)^dag t^dag
+    {1, 1, 1, 1, 3, 0, 0, 1, 1, 1},  // acc += Z_k(x+nu)^dag t^dag
     {0, 0, 3, 0, 0, 1, 4, 0, 0, 0},  // t  = U_nu(x-k) U_k(x-k+nu)
-    {2, 0, 0, 1, 1, 1, 3, 1, 1, 1},  // acc += t^dag Z_k(x-k)^dag
+    {3, 0, 0, 1, 1, 1, 3, 1, 1, 1},  // acc += t^dag Z_k(x-k)^dag
     {1, 1, 4, 0, 0, 0, 3, 1, 0, 0},  // t  = Z_k(x-k+nu) U_nu(x-k)^dag
     {0, 1, 4, 1, 1, 0, 3, 0, 0, 1},  // t += U_k(x-k+nu)^dag Z_nu(x-k)
-    {2, 0, 0, 0, 0, 1, 3, 0, 1, 1},  // acc += t U_k(x-k)
+    {3, 0, 0, 0, 0, 1, 3, 0, 1, 1},  // acc += t U_k(x-k)
 };
 
 template <bool FORCE>
@@ -333,7 +335,7 @@ __global__ void __launch_bounds__(128, GF_MINB_ADJ(dfl))
     ss.x[3] = nbr_rt(g, st, K, -1);
     ss.x[4] = nbr2_rt(g, st, K, -1, nu, +1);
 #pragma unroll 1
-    for (int q = 0; q < 10; ++q) df_exec(c_gather_ops[q], sm, tid, U, Z, V, nu, K, ss);
+    for (int q = 0; q < 10; ++q) df_exec(c_gather_ops[q], sm, tid, DfFields{{U, Z, Z}}, V, nu, K, ss);
   }
   if (!live) return;
   mat3<dfl> d = LinkFull<dfl>::load(Dp, nu, s, V);
@@ -355,11 +357,11 @@ __global__ void __launch_bounds__(128, GF_MINB_ADJ(dfl))
 // dS/dU order as add_staple_pair does; op 4 forms U S; op 5 e^Q U.
 __constant__ DfOp c_stout_ops[6] = {
     {0, 1, 1, 0, 0, 0, 2, 1, 0, 0},  // t  = U_nu(x+mu) U_mu(x+nu)^dag
-    {2, 0, 0, 0, 0, 1, 0, 1, 1, 1},  // acc += t U_nu(x)^dag
+    {3, 0, 0, 0, 0, 1, 0, 1, 1, 1},  // acc += t U_nu(x)^dag
     {0, 1, 3, 1, 0, 0, 4, 1, 0, 0},  // t  = U_nu(x+mu-nu)^dag U_mu(x-nu)^dag
-    {2, 0, 0, 0, 0, 1, 4, 0, 1, 1},  // acc += t U_nu(x-nu)
-    {0, 0, 0, 0, 3, 0, 0, 0, 0, 0},  // t  = U_mu(x) S
-    {2, 0, 0, 0, 0, 0, 0, 0, 1, 0},  // acc = e^Q U_mu(x)   (slot 0 holds e^Q by then)
+    {3, 0, 0, 0, 0, 1, 4, 0, 1, 1},  // acc += t U_nu(x-nu)
+    {0, 0, 0, 0, 4, 0, 0, 0, 0, 0},  // t  = U_mu(x) S
+    {3, 0, 0, 0, 0, 0, 0, 0, 1, 0},  // acc = e^Q U_mu(x)   (slot 0 holds e^Q by then)
 };
 
 __global__ void __launch_bounds__(128, GF_MINB(dfl))
@@ -392,10 +394,123 @@ __global__ void __launch_bounds__(128, GF_MINB(dfl))
       slot_store(sm, 0, tid, expiq(qh));
       if (Cout && live) LinkFull<dfl>::store(Cout, mu, s, V, scale(rho, dag(slot_load(sm, 1, tid))));
     }
-    df_exec(c_stout_ops[q < 12 ? (q & 3) : q - 8], sm, tid, U, U, V, mu, nu, ss);
+    df_exec(c_stout_ops[q < 12 ? (q & 3) : q - 8], sm, tid, DfFields{{U, U, U}}, V, mu, nu, ss);
   }
   if (live) LinkFull<dfl>::store(Uout, mu, s, V, slot_load(sm, 1, tid));
 }
+
+// The local adjoint: F0 = U, F1 = Dbar (or the top level's smeared links),
+// F2 = the stored C; d0 = mu, d1 = nu; sites x, x+mu, x+nu, x+mu-nu, x-nu.
+// Slots: 0 work (U C^dag, then Gamma, then Y), 1 Qh, 2 Qh^2 then e^Q,
+// 3 Lambda then Z then Dp, 4 Dbar of the top level, 5 a recomputed C.
+// Operand codes 14 and 15 stand for C and Dbar, resolved per launch.
+#define GF_LOCAL_SLOTS 6
+__constant__ DfOp c_local_ops[31] = {
+    // 0-11: S_mu of F0 into slot 5 (C recomputed), in dS/dU order
+    {0, 1, 1, 0, 0, 0, 2, 1, 0, 0}, {3, 0, 0, 0, 0, 1, 0, 1, 5, 1},
+    {0, 1, 3, 1, 0, 0, 4, 1, 0, 0}, {3, 0, 0, 0, 0, 1, 4, 0, 5, 1},
+    {0, 1, 1, 0, 0, 0, 2, 1, 0, 0}, {3, 0, 0, 0, 0, 1, 0, 1, 5, 1},
+    {0, 1, 3, 1, 0, 0, 4, 1, 0, 0}, {3, 0, 0, 0, 0, 1, 4, 0, 5, 1},
+    {0, 1, 1, 0, 0, 0, 2, 1, 0, 0}, {3, 0, 0, 0, 0, 1, 0, 1, 5, 1},
+    {0, 1, 3, 1, 0, 0, 4, 1, 0, 0}, {3, 0, 0, 0, 0, 1, 4, 0, 5, 1},
+    // 12-23: S_mu of F1 into slot 4 (top level: Dbar = beta/2 S)
+    {1, 1, 1, 0, 1, 0, 2, 1, 0, 0}, {3, 0, 0, 0, 1, 1, 0, 1, 4, 1},
+    {1, 1, 3, 1, 1, 0, 4, 1, 0, 0}, {3, 0, 0, 0, 1, 1, 4, 0, 4, 1},
+    {1, 1, 1, 0, 1, 0, 2, 1, 0, 0}, {3, 0, 0, 0, 1, 1, 0, 1, 4, 1},
+    {1, 1, 3, 1, 1, 0, 4, 1, 0, 0}, {3, 0, 0, 0, 1, 1, 4, 0, 4, 1},
+    {1, 1, 1, 0, 1, 0, 2, 1, 0, 0}, {3, 0, 0, 0, 1, 1, 0, 1, 4, 1},
+    {1, 1, 3, 1, 1, 0, 4, 1, 0, 0}, {3, 0, 0, 0, 1, 1, 4, 0, 4, 1},
+    {14, 0, 0, 0, 0, 0, 0, 1, 0, 0},  // 24: work = C U^dag
+    {0, 0, 0, 0, 15, 0, 0, 0, 3, 0},  // 25: Lambda = U Dbar
+    {4, 0, 0, 0, 6, 0, 0, 0, 0, 0},   // 26: work = Qh Lambda
+    {6, 0, 0, 0, 4, 0, 0, 0, 0, 1},   // 27: work += Lambda Qh
+    {0, 0, 0, 1, 3, 0, 0, 0, 3, 0},   // 28: Z = U^dag Y
+    {15, 0, 0, 0, 5, 0, 0, 0, 3, 0},  // 29: Dp = Dbar e^Q
+    {14, 0, 0, 1, 3, 0, 0, 1, 3, 1},  // 30: Dp += C^dag Y^dag
+};
+
+template <bool TOP>
+__global__ void __launch_bounds__(128, GF_MINB_ADJ(dfl))
+    k_bwd_local_df(const double2* __restrict__ U, const double2* __restrict__ F1, const double2* __restrict__ Cst,
+                   double2* __restrict__ Zout, double2* __restrict__ Dpout, Geom g, dfl rho, dfl halfbeta) {
+  extern __shared__ float sm[];  // GF_LOCAL_SLOTS slots of 36 x 128 floats
+  const int tid = threadIdx.x;
+  int s, mu;
+  link_of_thread(s, mu);
+  const bool live = s < g.vol;
+  const int V = g.vol;
+  const int sc = live ? s : 0;
+  const Site st = site_of(g, sc);
+  const bool recompute = Cst == nullptr;
+  const DfFields F{{U, F1, Cst ? Cst : U}};
+  DfSites ss;
+  ss.x[0] = sc;
+  ss.x[1] = nbr_rt(g, st, mu, +1);
+  int nu = 0;
+  ch_coef<dfl> cc;
+#pragma unroll 1
+  for (int q = 0; q < 31; ++q) {
+    if (q < 12 && !recompute) continue;
+    if (q >= 12 && q < 24 && !TOP) continue;
+    if (q < 24) {
+      const int r = q < 12 ? q : q - 12;
+      if ((r & 3) == 0) {
+        nu = (mu + 1 + (r >> 2)) & 3;
+        ss.x[2] = nbr_rt(g, st, nu, +1);
+        ss.x[3] = nbr2_rt(g, st, mu, +1, nu, -1);
+        ss.x[4] = nbr_rt(g, st, nu, -1);
+      }
+      if (r == 0) slot_store(sm, q < 12 ? 5 : 4, tid, zero3<dfl>());
+    }
+    DfOp op = c_local_ops[q];
+    if (op.a_src == 14) op.a_src = recompute ? 8 : 2;
+    if (op.b_src == 14) op.b_src = recompute ? 8 : 2;
+    if (op.a_src == 15) op.a_src = TOP ? 7 : 1;
+    if (op.b_src == 15) op.b_src = TOP ? 7 : 1;
+    df_exec(op, sm, tid, F, V, mu, nu, ss);
+    if (q == 11) slot_store(sm, 5, tid, scale(rho, dag(slot_load(sm, 5, tid))));  // C = rho S^dag
+    if (q == 23) slot_store(sm, 4, tid, scale(halfbeta, slot_load(sm, 4, tid)));  // Dbar = beta/2 S
+    if (q == 24) {
+      // Qh = -i TA(C U^dag)
+      const mat3<dfl> qh = times_i(dfl(-1), ta_proj(slot_load(sm, 0, tid)));
+      dfl c0, c1;
+      herm_invariants(qh, c0, c1);
+      ch_coefficients<dfl, true>(c0, c1, cc);
+      slot_store(sm, 1, tid, qh);
+      slot_store(sm, 2, tid, herm_square(qh));
+    }
+    if (q == 27) {
+      const mat3<dfl> lam = slot_load(sm, 3, tid), qh = slot_load(sm, 1, tid), qh2 = slot_load(sm, 2, tid);
+      mat3<dfl> gam = slot_load(sm, 0, tid);
+      const cplx<dfl> trL = trace(lam), trLQ = tr_nn(lam, qh), trLQ2 = tr_nn(lam, qh2);
+      const cplx<dfl> trB1 = cc.b1[0] * trL + cc.b1[1] * trLQ + cc.b1[2] * trLQ2;
+      const cplx<dfl> trB2 = cc.b2[0] * trL + cc.b2[1] * trLQ + cc.b2[2] * trLQ2;
+      mat3<dfl> E;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          cplx<dfl> v = cc.f[2] * gam.e[i][j];
+          fma_(v, cc.f[1], lam.e[i][j]);
+          fma_(v, trB1, qh.e[i][j]);
+          fma_(v, trB2, qh2.e[i][j]);
+          gam.e[i][j] = v;
+          cplx<dfl> w = cc.f[1] * qh.e[i][j];
+          fma_(w, cc.f[2], qh2.e[i][j]);
+          if (i == j) w = w + cc.f[0];
+          E.e[i][j] = w;
+        }
+      slot_store(sm, 0, tid, ta_proj(times_i(dfl(-1), gam)));  // Y
+      slot_store(sm, 2, tid, E);                                // e^Q
+    }
+    if (q == 28 && live) LinkFull<dfl>::store(Zout, mu, s, V, slot_load(sm, 3, tid));
+  }
+  if (live) LinkFull<dfl>::store(Dpout, mu, s, V, slot_load(sm, 3, tid));
+}
+
+#ifndef GF_DF_LOCAL_LOOP
+#define GF_DF_LOCAL_LOOP 1
+#endif
 
 #ifndef GF_DF_GATHER_LOOP
 #define GF_DF_GATHER_LOOP 1
@@ -481,7 +596,15 @@ static void backward_impl(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, do
     const ME* din = (l == st->nlev - 1) ? dbar : (const ME*)st->D[cur]->ptr;
     {
     ProfScope prof(ctx, kclass<R>(GF_K_BWD_LOCAL, GF_K_BWD_LOCAL64, GF_K_BWD_LOCAL_DF));
-    if (top) {
+    if constexpr (GF_DF_LOCAL_LOOP && std::is_same<R, dfl>::value) {
+      const size_t smem = (size_t)GF_LOCAL_SLOTS * 36 * 128 * sizeof(float);
+      auto kern = top ? k_bwd_local_df<true> : k_bwd_local_df<false>;
+      GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      kern<<<grid, 128, smem, ctx->stream>>>((const double2*)st->lev_in[l]->ptr,
+                                             top ? (const double2*)st->lev_in[l + 1]->ptr : (const double2*)din,
+                                             (const double2*)Cst, (double2*)st->Z->ptr, (double2*)st->Dp->ptr,
+                                             ctx->geom, (R)st->rho[l], (R)(0.5 * beta));
+    } else if (top) {
       k_bwd_local<R, true><<<grid, 128, 0, ctx->stream>>>(src_of<R>(st->lev_in[l]), src_of<R>(st->lev_in[l + 1]),
                                                           nullptr, Cst, (ME*)st->Z->ptr, (ME*)st->Dp->ptr, ctx->geom,
                                                           (R)st->rho[l], (R)(0.5 * beta));
