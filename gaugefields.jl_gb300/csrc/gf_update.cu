@@ -32,8 +32,14 @@ __global__ void __launch_bounds__(128) k_link_update(const double2* Uin, double2
   mat3<R> q = herm_from_coeffs(p);
   mat3<R> e = expiq(q);
   mat3<R> u = LinkFull<R>::load(Uin, mu, s, V);
-  mat3<R> w = mul_nn(e, u);
-  if (reunit) reunitarize(w);
+  // re-unitarisation rebuilds row 3 from rows 1-2, so only those are formed
+  mat3<R> w;
+  if (reunit) {
+    w = mul_nn_rows12(e, u);
+    reunitarize(w);
+  } else {
+    w = mul_nn(e, u);
+  }
   LinkFull<R>::store(Uout, mu, s, V, w);
   if (sh32) {
     mat3<float> f;

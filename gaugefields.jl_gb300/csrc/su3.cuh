@@ -560,11 +560,11 @@ GF_HD dfl dacc_get(const dacc& a) { return df_two_sum(a.s, a.c); }
 // that indexed the caller's matrices through pointers or dynamic indices came
 // out wrong under nvcc 13.0 -O3 (products of matrices built in registers read
 // stale values).
-template <bool DA, bool DB, bool ACC>
+template <bool DA, bool DB, bool ACC, int ROWS = 3>
 GF_HD mat3<dfl> df_matmul(const mat3<dfl>& a, const mat3<dfl>& b, const mat3<dfl>* c) {
   mat3<dfl> r;
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
+  for (int i = 0; i < ROWS; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       dacc re, im;
@@ -586,6 +586,26 @@ GF_HD mat3<dfl> df_matmul(const mat3<dfl>& a, const mat3<dfl>& b, const mat3<dfl
       r.e[i][j] = mk(dacc_get(re), dacc_get(im));
     }
   return r;
+}
+
+// Rows 1-2 of A*B (row 3 left zero), for updates that re-unitarise right
+// after the product: re-unitarisation rebuilds row 3 from rows 1-2.
+template <typename R>
+GF_HD mat3<R> mul_nn_rows12(const mat3<R>& a, const mat3<R>& b) {
+  mat3<R> r = zero3<R>();
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      cplx<R> v = a.e[i][0] * b.e[0][j];
+      fma_(v, a.e[i][1], b.e[1][j]);
+      fma_(v, a.e[i][2], b.e[2][j]);
+      r.e[i][j] = v;
+    }
+  return r;
+}
+__device__ __forceinline__ mat3<dfl> mul_nn_rows12(const mat3<dfl>& a, const mat3<dfl>& b) {
+  return df_matmul<false, false, false, 2>(a, b, nullptr);
 }
 
 template <bool DA, bool DB>
