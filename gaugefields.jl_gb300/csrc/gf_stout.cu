@@ -93,8 +93,12 @@ __global__ void __launch_bounds__(128, GF_MINB(R))
   // Omega = rho (U S)^dag, Q = TA(Omega) = -rho TA(U S), exp(Q) = exp(i Qh), Qh = i rho TA(U S)
   mat3<R> M = mul_nn(u, S);
   mat3<R> qh = times_i(rho, ta_proj(M));
-  mat3<R> E = expiq(qh);
-  Prec<R>::store_link(Uout, mu, s, V, mul_nn(E, u));
+  if constexpr (std::is_same<R, float>::value) {
+    // 12-real output: rows 1-2 of e^Q U are all that is stored
+    Prec<R>::store_link(Uout, mu, s, V, mul_nn_rows12(expiq<R, 2>(qh), u));
+  } else {
+    Prec<R>::store_link(Uout, mu, s, V, mul_nn(expiq(qh), u));
+  }
   if (Cout) LinkFull<R>::store(Cout, mu, s, V, scale(rho, dag(S)));
 }
 

@@ -30,15 +30,14 @@ __global__ void __launch_bounds__(128) k_link_update(const double2* Uin, double2
 #pragma unroll
   for (int a = 0; a < 8; ++a) p[a] = eps * from_f64<R>(P[((size_t)mu * 8 + a) * V + s]);
   mat3<R> q = herm_from_coeffs(p);
-  mat3<R> e = expiq(q);
   mat3<R> u = LinkFull<R>::load(Uin, mu, s, V);
   // re-unitarisation rebuilds row 3 from rows 1-2, so only those are formed
   mat3<R> w;
   if (reunit) {
-    w = mul_nn_rows12(e, u);
+    w = mul_nn_rows12(expiq<R, 2>(q), u);
     reunitarize(w);
   } else {
-    w = mul_nn(e, u);
+    w = mul_nn(expiq(q), u);
   }
   LinkFull<R>::store(Uout, mu, s, V, w);
   if (sh32) {

@@ -503,16 +503,18 @@ GF_HD void herm_invariants(const mat3<R>& q, R& c0, R& c1) {
 }
 
 // exp(iQ) for traceless Hermitian Q. Q2 receives Q^2 (callers reuse it).
-template <typename R>
+// ROWS = 2 forms rows 1-2 only (row 3 left zero), for products whose row 3 is
+// rebuilt or not stored.
+template <typename R, int ROWS = 3>
 __device__ __forceinline__ mat3<R> expiq(const mat3<R>& q, mat3<R>* q2out = nullptr) {
   R c0, c1;
   herm_invariants(q, c0, c1);
   ch_coef<R> cc;
   ch_coefficients<R, false>(c0, c1, cc);
   mat3<R> q2 = herm_square(q);
-  mat3<R> e;
+  mat3<R> e = zero3<R>();
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
+  for (int i = 0; i < ROWS; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       cplx<R> v = cc.f[1] * q.e[i][j];
