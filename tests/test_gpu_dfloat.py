@@ -123,3 +123,30 @@ def test_custom_integrator_uses_the_driver_precision(pkg, prec):
     tol = 1e-4 if prec == "mixed" else 1e-10
     assert abs(r1.delta_hamiltonian - r2.delta_hamiltonian) < tol
     assert np.abs(U.to_host() - U2.to_host()).max() < (1e-5 if prec == "mixed" else 1e-11)
+
+
+def test_md_step_entry_points_validate_arguments(pkg):
+    """gf_md_mom_update / gf_md_link_update reject what update_momenta! and
+    update_gaugefields! reject (ArgumentError), without touching the fields."""
+    import ctypes
+    from gaugefields_gb300 import _lib
+    lib = _lib.load()
+    U = pkg.gauge_configuration(L4, start="hot", seed=2)
+    P = pkg.gaussian_momenta(U, seed=3)
+    U0, P0 = U.to_host(), P.to_host()
+    drv = _driver(pkg, U, 6.0, "dfloat", rho=(0.1,))
+    prm = drv.params()
+    nan = ctypes.c_double(float("nan"))
+    assert lib.gf_md_mom_update(U.ctx.h, P.field.h, U.field.h, nan, ctypes.byref(prm)) == _lib.GF_EINVAL
+    assert lib.gf_md_link_update(U.ctx.h, U.field.h, P.field.h, nan, ctypes.byref(prm)) == _lib.GF_EINVAL
+    # kinds swapped
+    assert lib.gf_md_mom_update(U.ctx.h, U.field.h, P.field.h, ctypes.c_double(0.1), ctypes.byref(prm)) == _lib.GF_EINVAL
+    bad = drv.params()
+    bad.precision = 7
+    assert lib.gf_md_link_update(U.ctx.h, U.field.h, P.field.h, ctypes.c_double(0.1), ctypes.byref(bad)) == _lib.GF_EINVAL
+    bad = drv.params()
+    bad.steps = 0
+    assert lib.gf_md_mom_update(U.ctx.h, P.field.h, U.field.h, ctypes.c_double(0.1), ctypes.byref(bad)) == _lib.GF_EINVAL
+    assert np.array_equal(U.to_host(), U0) and np.array_equal(P.to_host(), P0)
+    with pytest.raises(ValueError):
+        pkg.update_momenta_(P, U, float("inf"), drv)

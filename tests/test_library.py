@@ -57,6 +57,10 @@ def test_null_arguments_are_rejected(pkg):
     assert lib.gf_plaquette(None, None, ctypes.byref(out)) == _lib.GF_EINVAL
     assert lib.gf_md_trajectory(None, None, None, None, None) == _lib.GF_EINVAL
     assert lib.gf_flow(None, None, ctypes.c_double(0.01), 1) == _lib.GF_EINVAL
+    prm = _lib.MDParams()
+    assert lib.gf_md_mom_update(None, None, None, ctypes.c_double(0.1), ctypes.byref(prm)) == _lib.GF_EINVAL
+    assert lib.gf_md_link_update(None, None, None, ctypes.c_double(0.1), ctypes.byref(prm)) == _lib.GF_EINVAL
+    assert lib.gf_stout_create(None, 2, None, _lib.GF_DFLOAT, 1, None) == _lib.GF_EINVAL
     assert lib.gf_field_free(None) == _lib.GF_OK
     assert lib.gf_ctx_destroy(None) == _lib.GF_OK
 
