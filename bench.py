@@ -292,30 +292,58 @@ def e2e_hmc(pkg, torch, L, steps, warmup, rank):
             "d2h_bytes_per_step": 36 * V * 16 + 3 * 8, "ms_per_step": 1e3 * sec / steps}
 
 
-def dh_check(pkg, L, ntherm, forms=("fp64", "mixed")):
-    """|Delta H_form - Delta H_fp64| for one trajectory from the same
-    configuration and momenta. The configuration is thermalised first: cold
-    start, then `ntherm` mixed-precision trajectories kept unconditionally."""
-    U, P, drv = make_setup(pkg, L, "mixed", SEED)
-    pkg._lib.call("gf_cold_start", U.ctx.h, U.field.h, ctx=U.ctx.h)
+def dh_study(pkg, torch, L, ntherm, ntraj, forms=("fp64", "mixed"), md_steps=None, start="cold"):
+    """|Delta H_form - Delta H_fp64| over `ntraj` trajectories, each from the
+    same thermalised configuration with the same fresh momenta in every form;
+    the Metropolis decisions use the same uniform. Thermalisation: a cold
+    (or Haar) start, then `ntherm` mixed trajectories kept unconditionally."""
+    import numpy as np
+    U, P, drv = make_setup(pkg, L, "mixed", SEED, md_steps)
+    if start == "cold":
+        pkg._lib.call("gf_cold_start", U.ctx.h, U.field.h, ctx=U.ctx.h)
+    t0 = time.perf_counter()
+    therm_seed = SEED + (5 if start == "cold" else 11)
     for t in range(ntherm):
-        pkg.gaussian_momenta_(P, seed=SEED + 5, sweep=t)
+        pkg.gaussian_momenta_(P, seed=therm_seed, sweep=t)
         pkg.md_trajectory_(U, P, drv)
-    Ut = U.to_host()
-    plaq = pkg.measure_plaquette(U)
-    res = {}
-    for prec in forms:
-        U2, P2, drv2 = make_setup(pkg, L, prec, SEED)
-        U2.from_host(Ut)
-        pkg.gaussian_momenta_(P2, seed=SEED, sweep=10 ** 6)
-        res[prec] = pkg.md_trajectory_(U2, P2, drv2).delta_hamiltonian
-        del U2, P2, drv2
-    out = {"dH_fp64": res["fp64"], "dH_mixed": res["mixed"], "abs_diff": abs(res["mixed"] - res["fp64"])}
-    if "dfloat" in res:
-        out["dH_dfloat"] = res["dfloat"]
-        out["abs_diff_dfloat"] = abs(res["dfloat"] - res["fp64"])
-    out["start"] = "cold start + %d mixed trajectories kept unconditionally (plaquette %.6f)" % (ntherm, plaq)
-    return out
+    t_therm = time.perf_counter() - t0
+    U0 = U.to_host()
+    plaq0 = pkg.measure_plaquette(U)
+    del U, P, drv
+    setups = {f: make_setup(pkg, L, f, SEED, md_steps) for f in forms}
+    rng = np.random.RandomState(2024)
+    rows = []
+    secs = {f: 0.0 for f in forms}
+    for i in range(ntraj):
+        u = rng.uniform()
+        r = {}
+        for f, (Uf, Pf, df) in setups.items():
+            Uf.from_host(U0)
+            pkg.gaussian_momenta_(Pf, seed=SEED + 1000, sweep=i)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            res = pkg.md_trajectory_(Uf, Pf, df)
+            secs[f] += time.perf_counter() - t1
+            r[f] = (res.delta_hamiltonian, pkg.measure_plaquette(Uf))
+        acc64 = u < np.exp(-r["fp64"][0])
+        row = {"dH_fp64": r["fp64"][0]}
+        for f in forms[1:]:
+            row["dH_" + f] = r[f][0]
+            row["abs_diff_" + f] = abs(r[f][0] - r["fp64"][0])
+            row["plaq_diff_" + f] = abs(r[f][1] - r["fp64"][1])
+            row["same_decision_" + f] = bool(acc64 == (u < np.exp(-r[f][0])))
+        rows.append(row)
+    out = {"lattice": [L] * 4, "md_steps": md_steps or NSTEPS, "trajectories": len(rows),
+           "start": "%s start + %d mixed trajectories kept unconditionally (plaquette %.6f)" % (start, ntherm, plaq0),
+           "therm_seconds": t_therm, "dH_fp64_median_abs": float(np.median([abs(x["dH_fp64"]) for x in rows])),
+           "seconds_per_trajectory": {f: secs[f] / len(rows) for f in forms}}
+    for f in forms[1:]:
+        d = [x["abs_diff_" + f] for x in rows]
+        out[f] = {"abs_dH_diff_median": float(np.median(d)), "abs_dH_diff_max": max(d),
+                  "within_1e-4": sum(v <= 1e-4 for v in d),
+                  "same_decision": sum(x["same_decision_" + f] for x in rows),
+                  "plaq_diff_max": max(x["plaq_diff_" + f] for x in rows)}
+    return out, rows
 
 
 def oracle_sample(threads, L_sample=16, md_steps=None):
@@ -388,60 +416,16 @@ def run_reference(args):
 
 
 def run_precision_mode(args):
-    """Mixed and double-float vs plain fp64 from one thermalised configuration:
-    thermalise with `--therm` mixed trajectories from a Haar start (kept
-    unconditionally), then `--steps` trajectories, each from that same
-    configuration with fresh momenta, in every form. Reports |dH_form -
-    dH_fp64|, the agreement of the Metropolis decisions under the same
-    uniform, the plaquette difference and each form's seconds per trajectory."""
-    import numpy as np
+    """Mixed and double-float vs plain fp64 from one thermalised configuration
+    (Haar start, `--therm` kept mixed trajectories), `--steps` trajectories
+    (dh_study); prints the summary with the per-trajectory rows."""
     import torch
     import __graft_entry__ as entry
     pkg = entry.build()
     L = args.lattice
-    U, P, drv = make_setup(pkg, L, "mixed", SEED, args.md_steps)
-    t0 = time.perf_counter()
-    for t in range(args.therm):
-        pkg.gaussian_momenta_(P, seed=SEED + 11, sweep=t)
-        pkg.md_trajectory_(U, P, drv)
-    t_therm = time.perf_counter() - t0
-    U0 = U.to_host()
-    plaq0 = pkg.measure_plaquette(U)
-    del U, P, drv
-    names = ("fp64", "mixed") + (() if args.no_dfloat else ("dfloat",))
-    forms = {f: make_setup(pkg, L, f, SEED, args.md_steps) for f in names}
-    rng = np.random.RandomState(2024)
-    rows = []
-    secs = {f: 0.0 for f in names}
-    for i in range(args.steps):
-        u = rng.uniform()
-        r = {}
-        for f, (Uf, Pf, df) in forms.items():
-            Uf.from_host(U0)
-            pkg.gaussian_momenta_(Pf, seed=SEED + 1000, sweep=i)
-            torch.cuda.synchronize()
-            t1 = time.perf_counter()
-            res = pkg.md_trajectory_(Uf, Pf, df)
-            secs[f] += time.perf_counter() - t1
-            r[f] = (res.delta_hamiltonian, pkg.measure_plaquette(Uf))
-        acc64 = u < np.exp(-r["fp64"][0])
-        row = {"dH_fp64": r["fp64"][0]}
-        for f in names[1:]:
-            row["dH_" + f] = r[f][0]
-            row["abs_diff_" + f] = abs(r[f][0] - r["fp64"][0])
-            row["plaq_diff_" + f] = abs(r[f][1] - r["fp64"][1])
-            row["same_decision_" + f] = bool(acc64 == (u < np.exp(-r[f][0])))
-        rows.append(row)
-    out = {"mode": "precision", "lattice": [L] * 4, "workload": workload_name(L), "md_steps": args.md_steps or NSTEPS,
-           "therm": args.therm, "therm_seconds": t_therm, "plaquette_start": plaq0, "trajectories": len(rows),
-           "dH_fp64_median_abs": float(np.median([abs(x["dH_fp64"]) for x in rows])),
-           "seconds_per_trajectory": {f: secs[f] / len(rows) for f in names}}
-    for f in names[1:]:
-        d = [x["abs_diff_" + f] for x in rows]
-        out[f] = {"abs_dH_diff_max": max(d), "abs_dH_diff_median": float(np.median(d)),
-                  "within_1e-4": sum(v <= 1e-4 for v in d),
-                  "same_decision": sum(x["same_decision_" + f] for x in rows),
-                  "plaq_diff_max": max(x["plaq_diff_" + f] for x in rows)}
+    forms = ("fp64", "mixed") + (() if args.no_dfloat else ("dfloat",))
+    out, rows = dh_study(pkg, torch, L, args.therm, args.steps, forms, args.md_steps, start="hot")
+    out = dict({"mode": "precision", "workload": workload_name(L), "therm": args.therm}, **out)
     out["rows"] = rows
     print(json.dumps(out))
     return 0
@@ -619,6 +603,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-dfloat", action="store_true", help="skip the double-float form's line")
     ap.add_argument("--md-steps", type=int, default=None, help="MD steps per trajectory (default 20)")
+    ap.add_argument("--dh-trajectories", type=int, default=5,
+                    help="trajectories of the Delta H comparison in the default line")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed", "dfloat"],
                     help="form of the force/link modes")
     ap.add_argument("--no-cpu", action="store_true")
@@ -683,7 +669,7 @@ def main():
                 "kernels_ms_per_step": {k: v["ms"] / 2 for k, v in kdf.items()}}
         del U, P, drv
     forms = ("fp64", "mixed") + (() if args.no_dfloat else ("dfloat",))
-    dh = dh_check(pkg, L, args.therm, forms) if not args.no_fp64 else None
+    dh = dh_study(pkg, torch, L, args.therm, args.dh_trajectories, forms)[0] if not args.no_fp64 else None
 
     e2e = None
     if not args.no_e2e:
