@@ -507,27 +507,42 @@ static void mom_update(gf_ctx* ctx, gf_field* P, const gf_field* U, const gf_fie
 }
 
 // The potential at the start of a trajectory is the one the previous MD call
-// ended on (accepted) or started from (rejected, links restored). It is reused
-// when a 64-bit hash of the fp64 links and the action parameters match, which
-// saves one fp64 stout forward + plaquette per trajectory; any change of the
-// links changes the hash, so a reused value is bitwise the recomputed one.
-static bool vcache_hit(const gf_ctx* ctx, const gf_md_params* p, unsigned long long h) {
-  if (!ctx->vc_valid || ctx->vc_hash != h || ctx->vc_beta != p->beta || ctx->vc_nstout != p->nstout ||
-      ctx->vc_precision != p->precision)
-    return false;
-  for (int l = 0; l < p->nstout; ++l)
-    if (ctx->vc_rho[l] != p->rho[l]) return false;
-  return true;
+// ended on (accepted) or started from (rejected: gf_hmc_update restores the
+// links, and a caller doing its own Metropolis around gf_md_trajectory
+// uploads or copies the old links back). Both are kept, each keyed by a
+// 64-bit hash of the fp64 links and the action parameters; a match saves one
+// stout forward + plaquette per trajectory. Any change of the links changes
+// the hash, so a reused value is bitwise the recomputed one.
+static bool vcache_lookup(const gf_ctx* ctx, const gf_md_params* p, unsigned long long h, double* V) {
+  for (int e = 0; e < 2; ++e) {
+    const auto& c = ctx->vc[e];
+    if (!c.valid || c.hash != h || c.beta != p->beta || c.nstout != p->nstout || c.precision != p->precision)
+      continue;
+    bool same = true;
+    for (int l = 0; l < p->nstout; ++l) same = same && c.rho[l] == p->rho[l];
+    if (same) {
+      *V = c.V;
+      return true;
+    }
+  }
+  return false;
 }
 
-static void vcache_set(gf_ctx* ctx, const gf_md_params* p, unsigned long long h, double V) {
-  ctx->vc_valid = 1;
-  ctx->vc_hash = h;
-  ctx->vc_V = V;
-  ctx->vc_beta = p->beta;
-  ctx->vc_nstout = p->nstout;
-  ctx->vc_precision = p->precision;
-  for (int l = 0; l < GF_MAX_STOUT; ++l) ctx->vc_rho[l] = l < p->nstout ? p->rho[l] : 0.0;
+static void vcache_clear(gf_ctx* ctx) {
+  ctx->vc[0].valid = 0;
+  ctx->vc[1].valid = 0;
+}
+
+// entry 0: the configuration an MD call ended on, entry 1: the one it started from
+static void vcache_set(gf_ctx* ctx, const gf_md_params* p, int e, unsigned long long h, double V) {
+  auto& c = ctx->vc[e];
+  c.valid = std::isfinite(V) ? 1 : 0;
+  c.hash = h;
+  c.V = V;
+  c.beta = p->beta;
+  c.nstout = p->nstout;
+  c.precision = p->precision;
+  for (int l = 0; l < GF_MAX_STOUT; ++l) c.rho[l] = l < p->nstout ? p->rho[l] : 0.0;
 }
 
 struct MDResult {
@@ -546,7 +561,7 @@ static MDResult md_run(gf_ctx* ctx, gf_field* U, gf_field* P, const gf_md_params
   }
   MDResult r;
   r.h0 = field_hash(ctx, U);
-  r.V0 = vcache_hit(ctx, p, r.h0) ? ctx->vc_V : potential(ctx, U, p);
+  if (!vcache_lookup(ctx, p, r.h0, &r.V0)) r.V0 = potential(ctx, U, p);
   r.H0 = r.V0 + 0.5 * kinetic(ctx, P);
   double eps = p->tau / p->steps;
   // Adjacent half steps of consecutive QPQ (PQP) steps act with the same P
@@ -672,10 +687,11 @@ extern "C" int gf_md_trajectory(gf_ctx* ctx, gf_field* U, gf_field* P, const gf_
   out[1] = r.H1;
   out[2] = r.H1 - r.H0;
   if (!std::isfinite(out[2])) {
-    ctx->vc_valid = 0;
+    vcache_clear(ctx);
     throw gf_error(GF_ENAN, "gf_md_trajectory: Delta H is not finite");
   }
-  vcache_set(ctx, prm, r.h1, r.V1);
+  vcache_set(ctx, prm, 0, r.h1, r.V1);
+  vcache_set(ctx, prm, 1, r.h0, r.V0);
   API_END(ctx)
 }
 
@@ -697,9 +713,8 @@ extern "C" int gf_hmc_update(gf_ctx* ctx, gf_field* U, gf_field* P, const gf_md_
   bool accept = finite && (h[2] <= 0.0 || unif < std::exp(-h[2]));
   if (!accept) copy_field(ctx, U, ctx->w_link64);
   GF_CUDA(cudaStreamSynchronize(ctx->stream));
-  if (accept) vcache_set(ctx, prm, r.h1, r.V1);
-  else if (std::isfinite(r.V0)) vcache_set(ctx, prm, r.h0, r.V0);
-  else ctx->vc_valid = 0;
+  vcache_set(ctx, prm, 0, r.h1, r.V1);
+  vcache_set(ctx, prm, 1, r.h0, r.V0);
   out[0] = h[0];
   out[1] = h[1];
   out[2] = h[2];

@@ -66,15 +66,17 @@ struct gf_ctx {
   gf_stout* w_stoutdf;    // double-float stack: mixed-form Hamiltonian (forward only) or GF_DFLOAT
   int w_stout_nlev;
   double w_stout_rho[GF_MAX_STOUT];
-  // potential of the last configuration an MD call ended on, keyed by a
-  // 64-bit hash of its fp64 links and the action parameters
+  // potentials of the configurations the last MD call started and ended on,
+  // keyed by a 64-bit hash of their fp64 links and the action parameters
   unsigned long long* d_hash;
   unsigned long long* h_hash;
-  int vc_valid;
-  unsigned long long vc_hash;
-  double vc_V, vc_beta;
-  int vc_nstout, vc_precision;
-  double vc_rho[GF_MAX_STOUT];
+  struct {
+    int valid;
+    unsigned long long hash;
+    double V, beta;
+    int nstout, precision;
+    double rho[GF_MAX_STOUT];
+  } vc[2];
   // staging buffer for host transfers in the reference layout (grown on demand)
   void* d_stage;
   size_t stage_bytes;

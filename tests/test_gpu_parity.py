@@ -413,6 +413,27 @@ def test_potential_reuse_is_bitwise_identical(pkg):
     assert r2.initial_hamiltonian - r1.final_hamiltonian != 0.0  # new momenta
 
 
+def test_potential_reuse_after_a_restored_rejection(pkg):
+    """A caller that rejects and uploads the old links back starts the next
+    trajectory from the configuration the previous one started from; that
+    potential is kept too, and reusing it is bitwise a fresh evaluation."""
+    U = pkg.gauge_configuration(L4, start="hot", seed=14)
+    U0 = U.to_host()
+    P = pkg.gaussian_momenta(U, seed=1)
+    drv = _smeared(pkg, U, 6.0, "mixed", steps=4)
+    r1 = pkg.md_trajectory_(U, P, drv)
+    U.from_host(U0)                                  # rejected: old links back
+    pkg.gaussian_momenta_(P, seed=1)
+    r2 = pkg.md_trajectory_(U, P, drv)
+    assert r2.initial_hamiltonian == r1.initial_hamiltonian
+    assert r2.delta_hamiltonian == r1.delta_hamiltonian
+    V = pkg.gauge_configuration(L4, start="cold")
+    V.from_host(U0)
+    Q = pkg.gaussian_momenta(V, seed=1)
+    r3 = pkg.md_trajectory_(V, Q, _smeared(pkg, V, 6.0, "mixed", steps=4))  # fresh context
+    assert r3.initial_hamiltonian == r1.initial_hamiltonian
+
+
 def test_flow(pkg, oracle):
     U = pkg.gauge_configuration(L4, start="hot", seed=9)
     Uh = U.to_host()
