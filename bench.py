@@ -648,6 +648,15 @@ def main():
     sec, launches, kern, dhs, acc = timed_hmc(pkg, torch, U, P, drv, args.steps, args.warmup, rank, dist, prof=True)
     clocks = clk.stop()
     del U, P, drv
+
+    # the same workload end to end through the C-ABI with host buffers, right
+    # after the device-resident timing (same GPU state)
+    e2e = None
+    if not args.no_e2e:
+        clk = ClockSampler(local)
+        clk.start()
+        e2e = e2e_hmc(pkg, torch, L, max(2, min(args.steps, 3)), 1, rank)
+        e2e["clocks"] = clk.stop()
     tmax = max_over_ranks(torch, dist, sec, "cuda")
     value = world * args.steps / tmax
 
@@ -671,9 +680,6 @@ def main():
     forms = ("fp64", "mixed") + (() if args.no_dfloat else ("dfloat",))
     dh = dh_study(pkg, torch, L, args.therm, args.dh_trajectories, forms)[0] if not args.no_fp64 else None
 
-    e2e = None
-    if not args.no_e2e:
-        e2e = e2e_hmc(pkg, torch, L, max(2, min(args.steps, 3)), 1, rank)
 
     # roofline of the dominant kernel (device time from CUDA events in the timed region)
     roof, compute = None, None
