@@ -127,7 +127,7 @@ def exact_exp_oracle(oracle):
     oracle.set_exp_method("eigen")
 
 
-def _config1(pkg, integrator, L=L8, seed=1234, reunit=False):
+def _hot8_trajectory(pkg, integrator, L=L8, seed=1234, reunit=False):
     U = pkg.gauge_configuration(L, start="hot", seed=seed)
     P = pkg.gaussian_momenta(U, seed=seed, sweep=0)
     Uh, Ph = U.to_host(), P.to_host()
@@ -140,11 +140,11 @@ def _config1(pkg, integrator, L=L8, seed=1234, reunit=False):
 
 
 @pytest.mark.parametrize("integrator", ["QPQ", "PQP"])
-def test_trajectory_config1(pkg, exact_exp_oracle, integrator):
+def test_trajectory_hot8_trajectory(pkg, exact_exp_oracle, integrator):
     """8^4 Haar start seed 1234, beta = 5.7, tau = 1, 10 steps, same momenta:
     Delta H to 1e-10, links and momenta to 1e-12 (Frobenius, per link)."""
     O = exact_exp_oracle
-    U, P, res, Uh, Ph = _config1(pkg, integrator)
+    U, P, res, Uh, Ph = _hot8_trajectory(pkg, integrator)
     h = O.md_trajectory(list(L8), Uh, Ph, 5.7, 1.0, 10, integrator)
     assert abs(res.initial_hamiltonian - h[0]) <= 1e-13 * abs(h[0])
     assert abs(res.delta_hamiltonian - h[2]) <= 1e-10
@@ -166,19 +166,19 @@ def test_omelyan_trajectory(pkg, exact_exp_oracle):
     assert frob_links(U.to_host(), Uh) < 1e-12
 
 
-def test_trajectory_config1_against_reference_eigen_exponential(pkg, oracle):
+def test_trajectory_8x4_beta57_against_reference_eigen_exponential(pkg, oracle):
     """The same trajectory against the reference's own eigen-method exptU!.
     That method is accurate to ~1e-14 per update (its eigenvectors come from
     differences of eigenvalues), and the hot-start MD amplifies the difference
     about 300-fold over tau = 1, so the bound here is 5e-11 on links."""
-    U, P, res, Uh, Ph = _config1(pkg, "QPQ")
+    U, P, res, Uh, Ph = _hot8_trajectory(pkg, "QPQ")
     h = oracle.md_trajectory(list(L8), Uh, Ph, 5.7, 1.0, 10, "QPQ")
     assert abs(res.delta_hamiltonian - h[2]) <= 2e-9
     assert frob_links(U.to_host(), Uh) < 5e-11
 
 
 def test_trajectory_with_reunitarisation_stays_within_parity(pkg, exact_exp_oracle):
-    U, P, res, Uh, Ph = _config1(pkg, "QPQ", L=L4, seed=3, reunit=True)
+    U, P, res, Uh, Ph = _hot8_trajectory(pkg, "QPQ", L=L4, seed=3, reunit=True)
     h = exact_exp_oracle.md_trajectory(list(L4), Uh, Ph, 5.7, 1.0, 10)
     assert abs(res.delta_hamiltonian - h[2]) <= 1e-10
     assert frob_links(U.to_host(), Uh) < 1e-12
@@ -279,7 +279,7 @@ def test_stout_recompute_matches_store(pkg):
 
 
 def test_stout_force_finite_differences(pkg):
-    """config 3(a): central differences, h = 1e-5, along 16 random su(3)
+    """Central differences, h = 1e-5, along 16 random su(3)
     directions at random links of a 4^4 lattice, of the GPU potential."""
     U = pkg.gauge_configuration(L4, start="hot", seed=7)
     U0 = U.to_host()
