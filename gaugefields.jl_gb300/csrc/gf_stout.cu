@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(128, GF_MINB_ADJ(R))
 
 // --------------------------------------------------------------------------
 // Double-float kernels as loops over tables of products. Inlined, every
-// double-float 3x3 product is about 2,500 instructions; the stout kernels hold
+// double-float 3x3 product is about 1,400 instructions; the stout kernels hold
 // 14-30 of them, overflow the instruction cache and stall on instruction
 // fetch (ncu). Here one product sits in the body of a run-time loop over a
 // table of operations. Each operand is a link of one of two fields (at one of
