@@ -150,3 +150,40 @@ def test_md_params_layout_matches_the_header(pkg, tmp_path):
     assert int(out["size"]) == ctypes.sizeof(_lib.MDParams)
     for f in fields:
         assert int(out[f]) == getattr(_lib.MDParams, f).offset, f
+
+
+def _df_tables():
+    """The double-float operation tables of gf_stout.cu: {name: [10-tuples]}."""
+    src = open(os.path.join(ROOT, "gaugefields.jl_gb300", "csrc", "gf_stout.cu")).read()
+    tables = {}
+    for m in re.finditer(r"__constant__ DfOp (c_\w+)\[(\d+)\] = \{(.*?)\n\};", src, re.S):
+        body = re.sub(r"//[^\n]*", "", m.group(3))
+        rows = [tuple(int(x) for x in r.split(",")) for r in re.findall(r"\{([^{}]*)\}", body)]
+        assert len(rows) == int(m.group(2)), m.group(1)
+        tables[m.group(1)] = rows
+    return src, tables
+
+
+def test_double_float_op_tables_stay_in_bounds():
+    """Every operand and result of the table-driven double-float kernels names
+    a field, a site, a direction or a shared-memory slot that the kernel has:
+    a slot index beyond the allocation would address shared memory out of
+    bounds."""
+    src, tables = _df_tables()
+    assert set(tables) == {"c_gather_ops", "c_stout_ops", "c_local_ops"}
+    nslots = {"c_gather_ops": 2, "c_stout_ops": 2,
+              "c_local_ops": int(re.search(r"#define GF_LOCAL_SLOTS (\d+)", src).group(1))}
+    # the static shared arrays of the two-slot kernels match
+    assert src.count("__shared__ float sm[2 * 36 * 128];") == 2
+    for name, rows in tables.items():
+        placeholders = {14, 15} if name == "c_local_ops" else set()
+        for r in rows:
+            assert len(r) == 10, (name, r)
+            a_src, a_dir, a_site, a_dag, b_src, b_dir, b_site, b_dag, out, acc = r
+            for src_, dir_, site, dag in ((a_src, a_dir, a_site, a_dag), (b_src, b_dir, b_site, b_dag)):
+                assert src_ in placeholders or 0 <= src_ < 3 + nslots[name], (name, r)
+                assert dir_ in (0, 1) and dag in (0, 1) and 0 <= site <= 4, (name, r)
+            assert 0 <= out < nslots[name] and acc in (0, 1), (name, r)
+    # the placeholders resolve to fields 1, 2 or slots 4, 5 (src 7, 8)
+    assert "recompute ? 8 : 2" in src and "TOP ? 7 : 1" in src
+    assert nslots["c_local_ops"] >= 6
