@@ -362,7 +362,17 @@ static gf_stout* stout_new(gf_ctx* ctx, int nlev, const double* rho, int precisi
   int lk = precision == GF_MIXED ? GF_LINK32 : GF_LINK64;
   int mk = precision == GF_MIXED ? GF_MAT32 : GF_MAT64;
   try {
-    for (int l = 1; l <= nlev; ++l) st->lev_in[l] = field_new(ctx, lk);
+    for (int l = 1; l <= nlev; ++l) {
+      if (fwd_only && l > 2) {
+        // a forward-only stack holds one level's input and output at a time:
+        // level l writes where level l - 2 wrote (two buffers in turn)
+        gf_field* a = new gf_field(*st->lev_in[l - 2]);
+        a->owned = 0;
+        st->lev_in[l] = a;
+      } else {
+        st->lev_in[l] = field_new(ctx, lk);
+      }
+    }
     if (fwd_only) {
       st->store = 0;  // forward only: no C, no back-propagation buffers
       st->fwd_only = 1;

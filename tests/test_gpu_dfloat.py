@@ -150,3 +150,16 @@ def test_md_step_entry_points_validate_arguments(pkg):
     assert np.array_equal(U.to_host(), U0) and np.array_equal(P.to_host(), P0)
     with pytest.raises(ValueError):
         pkg.update_momenta_(P, U, float("inf"), drv)
+
+
+@pytest.mark.parametrize("nlev", [3, 4])
+def test_hamiltonian_with_alternating_level_buffers(pkg, nlev):
+    """The mixed form's Hamiltonian smears with a forward-only double-float
+    stack whose levels beyond the second reuse two buffers in turn; with 3 and
+    4 levels it equals the fp64 Hamiltonian to 1e-13."""
+    U = pkg.gauge_configuration(L4, start="hot", seed=19)
+    P = pkg.gaussian_momenta(U, seed=20)
+    rho = (0.1, 0.08, 0.12, 0.1)[:nlev]
+    h = {prec: pkg.md_hamiltonian(U, P, _driver(pkg, U, 6.0, prec, rho=rho)) for prec in ("fp64", "mixed", "dfloat")}
+    assert abs(h["mixed"] - h["fp64"]) <= 1e-13 * abs(h["fp64"])
+    assert abs(h["dfloat"] - h["fp64"]) <= 1e-13 * abs(h["fp64"])
