@@ -144,6 +144,8 @@ extern "C" int gf_ctx_destroy(gf_ctx* ctx) {
   if (ctx->h_result) cudaFreeHost(ctx->h_result);
   if (ctx->d_hash) cudaFree(ctx->d_hash);
   if (ctx->d_stage) cudaFree(ctx->d_stage);
+  for (int i = 0; i < 2; ++i)
+    if (ctx->arena[i]) cudaFree(ctx->arena[i]);
   if (ctx->h_hash) cudaFreeHost(ctx->h_hash);
   if (ctx->prof_ev) {
     for (int i = 0; i < 2 * GF_PROF_CAP; ++i) cudaEventDestroy(ctx->prof_ev[i]);
@@ -348,7 +350,7 @@ extern "C" int gf_staple(gf_ctx* ctx, const gf_field* U, int mu, gf_field* V) {
 // stout workspace
 // ---------------------------------------------------------------------------
 static gf_stout* stout_new(gf_ctx* ctx, int nlev, const double* rho, int precision, int store,
-                           bool fwd_only = false) {
+                           bool fwd_only = false, bool arena = false) {
   need(nlev >= 1 && nlev <= GF_MAX_STOUT, "stout: number of levels must be 1..GF_MAX_STOUT");
   need(precision == GF_FP64 || precision == GF_MIXED || precision == GF_DFLOAT,
        "stout: precision must be GF_FP64, GF_MIXED or GF_DFLOAT");
@@ -363,7 +365,9 @@ static gf_stout* stout_new(gf_ctx* ctx, int nlev, const double* rho, int precisi
   int mk = precision == GF_MIXED ? GF_MAT32 : GF_MAT64;
   try {
     for (int l = 1; l <= nlev; ++l) {
-      if (fwd_only && l > 2) {
+      if (fwd_only && arena && l <= 2) {
+        st->lev_in[l] = arena_view(ctx, l - 1, 0, lk);
+      } else if (fwd_only && l > 2) {
         // a forward-only stack holds one level's input and output at a time:
         // level l writes where level l - 2 wrote (two buffers in turn)
         gf_field* a = new gf_field(*st->lev_in[l - 2]);
@@ -380,10 +384,19 @@ static gf_stout* stout_new(gf_ctx* ctx, int nlev, const double* rho, int precisi
     }
     if (st->store)
       for (int l = 0; l < nlev; ++l) st->C[l] = field_new(ctx, mk);
-    st->Z = field_new(ctx, mk);
-    st->Dp = field_new(ctx, mk);
-    st->D[0] = field_new(ctx, mk);
-    st->D[1] = field_new(ctx, mk);
+    if (arena && mk == GF_MAT32) {
+      // two fp32 matrix fields fill one fp64 link-sized block
+      const size_t half = field_bytes(ctx->geom, GF_MAT32);
+      st->Z = arena_view(ctx, 0, 0, mk);
+      st->Dp = arena_view(ctx, 0, half, mk);
+      st->D[0] = arena_view(ctx, 1, 0, mk);
+      st->D[1] = arena_view(ctx, 1, half, mk);
+    } else {
+      st->Z = field_new(ctx, mk);
+      st->Dp = field_new(ctx, mk);
+      st->D[0] = field_new(ctx, mk);
+      st->D[1] = field_new(ctx, mk);
+    }
   } catch (...) {
     gf_stout_destroy(st);
     throw;
@@ -476,7 +489,8 @@ static gf_stout* ctx_stout(gf_ctx* ctx, const gf_md_params* p, int precision) {
   if (!same) {
     if (*slot) gf_stout_destroy(*slot);
     *slot = nullptr;
-    *slot = stout_new(ctx, p->nstout, p->rho, precision, store, fwd_only);
+    // the mixed form's two internal stacks share the context's scratch blocks
+    *slot = stout_new(ctx, p->nstout, p->rho, precision, store, fwd_only, p->precision == GF_MIXED);
   }
   return *slot;
 }

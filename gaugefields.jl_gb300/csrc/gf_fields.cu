@@ -38,6 +38,27 @@ gf_field* field_new(gf_ctx* ctx, int kind) {
   return f;
 }
 
+gf_field* arena_view(gf_ctx* ctx, int which, size_t off, int kind) {
+  const size_t cap = field_bytes(ctx->geom, GF_LINK64);
+  if (!ctx->arena[which]) {
+    cudaError_t e = cudaMalloc(&ctx->arena[which], cap);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      ctx->arena[which] = nullptr;
+      throw gf_error(GF_ENOMEM, "cudaMalloc of " + std::to_string(cap) + " bytes failed: " + cudaGetErrorString(e));
+    }
+  }
+  const size_t bytes = field_bytes(ctx->geom, kind);
+  if (off + bytes > cap) throw gf_error(GF_EINVAL, "scratch view beyond its block");
+  gf_field* f = new gf_field;
+  f->ctx = ctx;
+  f->kind = kind;
+  f->ptr = (char*)ctx->arena[which] + off;
+  f->bytes = bytes;
+  f->owned = 0;
+  return f;
+}
+
 void field_delete(gf_field* f) {
   if (!f) return;
   if (f->owned && f->ptr) cudaFree(f->ptr);

@@ -61,6 +61,11 @@ struct gf_ctx {
   gf_field* w_link64b;    // W2 of the flow
   gf_field* w_mom[4];     // F0, F1, F2, Ftmp of the RK3 flow (fp64 coefficients)
   gf_field* w_link32;     // fp32 12-real shadow of the thin links (mixed form)
+  // Two scratch blocks of one fp64 link field each, shared by the mixed form's
+  // internal stacks: the Hamiltonian's double-float level buffers and the
+  // force adjoint's Z, Dp, D[0], D[1] (fp32). They are never live together:
+  // the potential runs before and after the MD steps, the adjoint within them.
+  void* arena[2];
   gf_stout* w_stout64;    // stout workspace, fp64
   gf_stout* w_stout32;    // stout workspace, fp32
   gf_stout* w_stoutdf;    // double-float stack: mixed-form Hamiltonian (forward only) or GF_DFLOAT
@@ -108,6 +113,8 @@ namespace gf {
 
 size_t field_bytes(const Geom& g, int kind);
 gf_field* field_new(gf_ctx* ctx, int kind);
+// a non-owning field of `kind` over scratch block `which` at byte offset `off`
+gf_field* arena_view(gf_ctx* ctx, int which, size_t off, int kind);
 void field_delete(gf_field* f);
 
 inline int blocks_for(int n, int bs) { return (n + bs - 1) / bs; }
