@@ -524,12 +524,15 @@ def run_scale_mode(args):
                           "staging buffer for host transfers, one fp64 link field, is not included)"}
     # the start configuration in the host layout, from a context of its own
     # so that the staging buffer of the transfer is gone before the
-    # measurements
-    Ut = pkg.gauge_configuration((L,) * 4, start="hot", seed=SEED)
-    U0 = Ut.to_host()
-    del Ut
-    torch.cuda.synchronize()
-    for recompute in (False, True):
+    # measurements (--device-only: no host copy; the timed trajectories then
+    # continue from the previous one instead of restarting from it)
+    U0 = None
+    if not args.device_only:
+        Ut = pkg.gauge_configuration((L,) * 4, start="hot", seed=SEED)
+        U0 = Ut.to_host()
+        del Ut
+        torch.cuda.synchronize()
+    for recompute in ((True,) if args.recompute_only else (False, True)):
         U, P, drv = setup("mixed", recompute)
         pkg.gaussian_momenta_(P, seed=SEED, sweep=0)
         torch.cuda.synchronize()
@@ -540,7 +543,8 @@ def run_scale_mode(args):
         used = total - torch.cuda.mem_get_info()[0] - (total - free0)
         secs = []
         for k in range(args.steps):
-            U.from_host(U0)
+            if U0 is not None:
+                U.from_host(U0)
             pkg.gaussian_momenta_(P, seed=SEED, sweep=k + 1)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -552,7 +556,7 @@ def run_scale_mode(args):
                     "first_trajectory_s": first}
         del U, P, drv
         torch.cuda.synchronize()
-    if args.no_fp64:
+    if args.no_fp64 or U0 is None:
         print(json.dumps(out))
         return 0
     # Delta H of the first trajectory in the plain fp64 form
@@ -614,6 +618,8 @@ def main():
     ap.add_argument("--md-steps", type=int, default=None, help="MD steps per trajectory (default 20)")
     ap.add_argument("--dh-trajectories", type=int, default=5,
                     help="trajectories of the Delta H comparison in the default line")
+    ap.add_argument("--device-only", action="store_true", help="scale mode: no host copies of the lattice")
+    ap.add_argument("--recompute-only", action="store_true", help="scale mode: only the recompute-C adjoint")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed", "dfloat"],
                     help="form of the force/link modes")
     ap.add_argument("--no-cpu", action="store_true")
