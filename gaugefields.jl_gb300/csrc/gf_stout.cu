@@ -316,8 +316,12 @@ __constant__ DfOp c_gather_ops[10] = {
     {3, 0, 0, 0, 0, 1, 3, 0, 1, 1},  // acc += t U_k(x-k)
 };
 
+// three blocks per SM: 168 registers without spills, 36 KB of shared memory each
+#ifndef GF_DF_GATHER_MINB
+#define GF_DF_GATHER_MINB 3
+#endif
 template <bool FORCE>
-__global__ void __launch_bounds__(128, GF_MINB_ADJ(dfl))
+__global__ void __launch_bounds__(128, GF_DF_GATHER_MINB)
     k_bwd_gather_df(const double2* __restrict__ U, const double2* __restrict__ Z, const double2* __restrict__ Dp,
                     double2* __restrict__ Dout, double* __restrict__ P, Geom g, dfl rho, double coef) {
   __shared__ float sm[2 * 36 * 128];
