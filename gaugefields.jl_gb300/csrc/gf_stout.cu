@@ -372,7 +372,12 @@ __constant__ DfOp c_stout_ops[6] = {
     {3, 0, 0, 0, 0, 0, 0, 0, 1, 0},  // acc = e^Q U_mu(x)   (slot 0 holds e^Q by then)
 };
 
-__global__ void __launch_bounds__(128, GF_MINB(dfl))
+// three blocks per SM (168 registers); four fit without spills at 128
+// registers but measured 4% slower
+#ifndef GF_DF_FWD_MINB
+#define GF_DF_FWD_MINB 3
+#endif
+__global__ void __launch_bounds__(128, GF_DF_FWD_MINB)
     k_stout_fwd_df(const double2* __restrict__ U, double2* __restrict__ Uout, double2* __restrict__ Cout, Geom g,
                    dfl rho) {
   __shared__ float sm[2 * 36 * 128];
