@@ -240,10 +240,11 @@ __global__ void __launch_bounds__(128, GF_MINB_ADJ(R))
 // double-float 3x3 product is about 1,400 instructions; the stout kernels hold
 // 14-30 of them, overflow the instruction cache and stall on instruction
 // fetch (ncu). Here one product sits in the body of a run-time loop over a
-// table of operations. Each operand is a link of one of two fields (at one of
-// up to five sites, in one of two directions) or a per-thread slot in shared
-// memory, optionally daggered; the result goes to a slot, optionally added
-// to it. Out-of-line forms of the product were slower (argument passing) or
+// table of operations. Each operand is a link of one of up to three fields
+// (at one of five sites, in one of two directions) or a per-thread slot in
+// shared memory, optionally daggered; the result goes to a slot, optionally
+// added to it. The order of the operations is that of the inlined kernels, so
+// the results are the same. Out-of-line forms of the product were slower (argument passing) or
 // miscompiled (pointers into the caller's registers), which this avoids.
 // --------------------------------------------------------------------------
 struct DfOp {
