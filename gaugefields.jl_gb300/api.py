@@ -27,7 +27,7 @@ __all__ = [
     "md_action_workspace", "update_gaugefields_", "update_momenta_", "md_step_", "md_trajectory_",
     "hmc_update_", "STOUT_Layer", "CovNeuralnet", "stout_smearing", "smear", "calc_smearedU", "back_prop",
     "Gradientflow", "gradient_flow", "flow_", "add_force_", "energy_density_plaquette", "substitute_U_",
-    "similar", "clear_U_",
+    "similar", "clear_U_", "save_configuration", "load_configuration_",
 ]
 
 
@@ -222,6 +222,41 @@ def gauge_configuration(lattice, backend=None, colors=3, halo=1, start="cold", s
         if seed is None:
             seed = int.from_bytes(os.urandom(8), "little")
         call("gf_hot_start", ctx.h, U.field.h, ctypes.c_uint64(int(seed)), ctx=ctx.h)
+    return U
+
+
+# ---------------------------------------------------------------------------
+# configuration files (src/API.jl:711-826)
+# ---------------------------------------------------------------------------
+def save_configuration(filename, U, format="ildg", precision="field", append=False):
+    """save_configuration(filename, U; format=:ildg, precision) (src/API.jl:711-726).
+
+    ILDG only: the links are downloaded in the reference layout and written
+    as one LIME message (ildg.py). precision "field" writes the fields' own
+    64 bits; 32 or 64 choose the stored reals. append=True adds the
+    configuration after the ones already in the file."""
+    if format != "ildg":
+        raise ValueError("format must be :ildg for the GB300 backend (JLD2 and Bridge output are not built); got %s"
+                         % format)
+    if precision == "field":
+        precision = 64
+    if precision not in (32, 64):
+        raise ValueError("ILDG precision must be :field, 32, or 64; got %r" % (precision,))
+    from . import ildg
+    ildg.write(filename, U.to_host(), U.L, precision, append=append)
+    return None
+
+
+def load_configuration_(U, filename, format="ildg", index=1):
+    """load_configuration!(U, filename; format=:ildg) (src/API.jl:784-826):
+    the configuration `index` of the file (1 = the first, as the reference
+    loads) into U, whose lattice must match the file's."""
+    if format != "ildg":
+        raise ValueError("format must be :ildg for the GB300 backend (JLD2 and Bridge input are not built); got %s"
+                         % format)
+    from . import ildg
+    links, _ = ildg.read(filename, L=U.L, index=index)
+    U.from_host(links)
     return U
 
 

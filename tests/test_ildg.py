@@ -1,0 +1,160 @@
+"""ILDG configuration files (save_configuration / load_configuration! with
+format=:ildg; src/API.jl:711-826, src/output/ildg_format.jl) on the host
+layout, against links from the oracle's Haar generator. CPU only, except the
+last test, which goes through a device configuration."""
+import struct
+
+import numpy as np
+import pytest
+
+import __graft_entry__ as entry
+
+L4 = (4, 4, 4, 4)
+L_MIXED = (4, 2, 6, 2)
+
+
+@pytest.fixture(scope="module")
+def io():
+    entry.load_package()
+    from gaugefields_gb300 import ildg as mod
+    return mod
+
+
+def _links(oracle, L, seed):
+    return oracle.hot_start(list(L), seed)
+
+
+def test_round_trip_fp64_is_exact(io, oracle, tmp_path):
+    U = _links(oracle, L_MIXED, 3)
+    f = tmp_path / "a.ildg"
+    io.write(str(f), U, L_MIXED, 64)
+    V, h = io.read(str(f), L=L_MIXED)
+    assert np.array_equal(V, U)
+    assert h["L"] == L_MIXED and h["precision"] == 64 and h["NC"] == 3
+
+
+def test_round_trip_fp32(io, oracle, tmp_path):
+    U = _links(oracle, L4, 4)
+    f = tmp_path / "b.ildg"
+    io.write(str(f), U, L4, 32)
+    V, h = io.read(str(f))
+    assert h["precision"] == 32
+    assert np.abs(V - U).max() < 1.2e-7
+    assert np.array_equal(V, U.astype(np.complex64).astype(np.complex128))
+
+
+def test_lime_structure_and_header(io, oracle, tmp_path):
+    U = _links(oracle, L_MIXED, 5)
+    f = tmp_path / "c.ildg"
+    io.write(str(f), U, L_MIXED, 64)
+    recs = io.read_records(str(f))
+    assert [r["type"] for r in recs] == ["ildg-format", "ildg-binary-data"]
+    assert recs[0]["mb"] and not recs[0]["me"] and not recs[1]["mb"] and recs[1]["me"]
+    assert all(r["message"] == 1 for r in recs) and [r["record"] for r in recs] == [1, 2]
+    raw = f.read_bytes()
+    assert len(raw) % 8 == 0
+    assert struct.unpack(">I", raw[:4])[0] == 0x456789AB
+    xml = raw[recs[0]["offset"]:recs[0]["offset"] + recs[0]["length"]].decode()
+    for tag, val in (("field", "su3gauge"), ("precision", "64"), ("lx", "4"), ("ly", "2"), ("lz", "6"), ("lt", "2")):
+        assert "<%s>%s</%s>" % (tag, val, tag) in xml
+    assert 'xmlns="http://www.lqcd.org/ildg"' in xml
+    V = int(np.prod(L_MIXED))
+    assert recs[1]["length"] == V * 4 * 9 * 16
+
+
+def test_payload_order_is_site_direction_row_column(io, oracle, tmp_path):
+    """x fastest over the sites, then directions x, y, z, t, then each matrix
+    row by row, real before imaginary, big-endian (ildg_format.jl:697-745)."""
+    U = _links(oracle, L_MIXED, 6)
+    f = tmp_path / "d.ildg"
+    io.write(str(f), U, L_MIXED, 64)
+    rec = io.read_records(str(f))[1]
+    raw = f.read_bytes()[rec["offset"]:rec["offset"] + rec["length"]]
+    NX, NY, NZ, NT = L_MIXED
+    for (x, y, z, t, mu, row, col) in ((0, 0, 0, 0, 0, 0, 0), (1, 0, 0, 0, 2, 1, 2), (3, 1, 5, 1, 3, 2, 0)):
+        lex = x + NX * (y + NY * (z + NZ * t))
+        k = (((lex * 4 + mu) * 3 + row) * 3 + col) * 2
+        re, im = struct.unpack(">dd", raw[8 * k:8 * k + 16])
+        # host layout: [mu, lex] holds the matrix column by column
+        assert (re, im) == (U[mu, lex, col, row].real, U[mu, lex, col, row].imag)
+
+
+def test_several_configurations_in_one_file(io, oracle, tmp_path):
+    A, B = _links(oracle, L4, 7), _links(oracle, L4, 8)
+    f = tmp_path / "e.ildg"
+    io.write(str(f), A, L4, 64)
+    io.write(str(f), B, L4, 32, append=True)
+    hs = io.headers(str(f))
+    assert [h["precision"] for h in hs] == [64, 32] and [h["message"] for h in hs] == [1, 2]
+    assert np.array_equal(io.read(str(f), index=1)[0], A)
+    assert np.abs(io.read(str(f), index=2)[0] - B).max() < 1.2e-7
+    with pytest.raises(ValueError):
+        io.read(str(f), index=3)
+
+
+def test_missing_precision_element_means_32(io, oracle, tmp_path):
+    """The reference's reader assumes precision 32 without the element."""
+    U = _links(oracle, L4, 9)
+    xml = io.format_xml(L4, 32).replace("  <precision>32</precision>\n", "").encode()
+    ordered = np.ascontiguousarray(np.transpose(np.swapaxes(U, -1, -2), (1, 0, 2, 3)))
+    payload = ordered.view(np.float64).reshape(-1).astype(">f4").tobytes()
+    f = tmp_path / "f.ildg"
+    with open(f, "wb") as fp:
+        io.write_records(fp, [("ildg-format", xml), ("ildg-binary-data", payload)])
+    V, h = io.read(str(f))
+    assert h["precision"] == 32 and np.abs(V - U).max() < 1.2e-7
+
+
+def test_rejections(io, oracle, tmp_path):
+    U = _links(oracle, L4, 10)
+    f = tmp_path / "g.ildg"
+    io.write(str(f), U, L4, 64)
+    with pytest.raises(ValueError):
+        io.read(str(f), L=(4, 4, 4, 2))           # lattice mismatch
+    bad = tmp_path / "h.ildg"
+    bad.write_bytes(b"\0" * 144)
+    with pytest.raises(ValueError):
+        io.read(str(bad))                          # not LIME
+    nofmt = tmp_path / "i.ildg"
+    with open(nofmt, "wb") as fp:
+        io.write_records(fp, [("ildg-binary-data", b"\0" * 16)])
+    with pytest.raises(ValueError):
+        io.read(str(nofmt))                        # no ildg-format record
+    short = tmp_path / "j.ildg"
+    with open(short, "wb") as fp:
+        io.write_records(fp, [("ildg-format", io.format_xml(L4, 64).encode()), ("ildg-binary-data", b"\0" * 64)])
+    with pytest.raises(ValueError):
+        io.read(str(short))                        # payload of the wrong size
+    with pytest.raises(ValueError):
+        io.write(str(f), U, L4, 16)                # precision
+
+
+def test_read_configuration_has_the_oracle_plaquette(io, oracle, tmp_path):
+    U = _links(oracle, L_MIXED, 11)
+    f = tmp_path / "k.ildg"
+    io.write(str(f), U, L_MIXED, 64)
+    V, _ = io.read(str(f))
+    assert oracle.plaquette(list(L_MIXED), V) == oracle.plaquette(list(L_MIXED), U)
+
+
+def test_package_exports_the_configuration_io(pkg):
+    assert callable(pkg.save_configuration) and callable(pkg.load_configuration_)
+    with pytest.raises(ValueError):
+        pkg.save_configuration("x.ildg", None, format="bridge")
+    with pytest.raises(ValueError):
+        pkg.load_configuration_(None, "x.ildg", format="jld2")
+
+
+@pytest.mark.gpu
+def test_save_and_load_through_the_device(pkg, tmp_path):
+    U = pkg.gauge_configuration(L_MIXED, start="hot", seed=21)
+    f = str(tmp_path / "dev.ildg")
+    pkg.save_configuration(f, U, format="ildg")
+    W = pkg.gauge_configuration(L_MIXED, start="cold")
+    pkg.load_configuration_(W, f, format="ildg")
+    assert np.array_equal(W.to_host(), U.to_host())
+    assert pkg.measure_plaquette(W) == pkg.measure_plaquette(U)
+    with pytest.raises(ValueError):
+        pkg.load_configuration_(pkg.gauge_configuration(L4, start="cold"), f, format="ildg")
+    with pytest.raises(ValueError):
+        pkg.save_configuration(f, U, format="jld2")
