@@ -229,14 +229,21 @@ def gauge_configuration(lattice, backend=None, colors=3, halo=1, start="cold", s
 # configuration files (src/API.jl:711-826)
 # ---------------------------------------------------------------------------
 def save_configuration(filename, U, format="ildg", precision="field", append=False):
-    """save_configuration(filename, U; format=:ildg, precision) (src/API.jl:711-726).
+    """save_configuration(filename, U; format=:ildg|:bridge, precision) (src/API.jl:711-726).
 
-    ILDG only: the links are downloaded in the reference layout and written
-    as one LIME message (ildg.py). precision "field" writes the fields' own
-    64 bits; 32 or 64 choose the stored reals. append=True adds the
-    configuration after the ones already in the file."""
+    The links are downloaded in the reference layout and written as one LIME
+    message (format "ildg", ildg.py) or as Bridge++ text (format "bridge",
+    bridge.py). For ILDG, precision "field" writes the fields' own 64 bits; 32
+    or 64 choose the stored reals; append=True adds the configuration after
+    the ones already in the file. Portable JLD2 output is not built."""
+    if format == "bridge":
+        if precision != "field" or append:
+            raise ValueError("Bridge output does not accept format keywords")
+        from . import bridge
+        bridge.write(filename, U.to_host(), U.L)
+        return None
     if format != "ildg":
-        raise ValueError("format must be :ildg for the GB300 backend (JLD2 and Bridge output are not built); got %s"
+        raise ValueError("format must be :ildg or :bridge for the GB300 backend (JLD2 output is not built); got %s"
                          % format)
     if precision == "field":
         precision = 64
@@ -248,11 +255,15 @@ def save_configuration(filename, U, format="ildg", precision="field", append=Fal
 
 
 def load_configuration_(U, filename, format="ildg", index=1):
-    """load_configuration!(U, filename; format=:ildg) (src/API.jl:784-826):
-    the configuration `index` of the file (1 = the first, as the reference
-    loads) into U, whose lattice must match the file's."""
+    """load_configuration!(U, filename; format=:ildg|:bridge) (src/API.jl:784-826):
+    for ILDG the configuration `index` of the file (1 = the first, as the
+    reference loads) into U, whose lattice must match the file's."""
+    if format == "bridge":
+        from . import bridge
+        U.from_host(bridge.read(filename, U.L))
+        return U
     if format != "ildg":
-        raise ValueError("format must be :ildg for the GB300 backend (JLD2 and Bridge input are not built); got %s"
+        raise ValueError("format must be :ildg or :bridge for the GB300 backend (JLD2 input is not built); got %s"
                          % format)
     from . import ildg
     links, _ = ildg.read(filename, L=U.L, index=index)

@@ -1,5 +1,6 @@
-"""ILDG configuration files (save_configuration / load_configuration! with
-format=:ildg; src/API.jl:711-826, src/output/ildg_format.jl) on the host
+"""ILDG and Bridge++ configuration files (save_configuration /
+load_configuration! with format=:ildg or :bridge; src/API.jl:711-826,
+src/output/ildg_format.jl, src/output/bridge_format.jl) on the host
 layout, against links from the oracle's Haar generator. CPU only, except the
 last test, which goes through a device configuration."""
 import struct
@@ -137,10 +138,35 @@ def test_read_configuration_has_the_oracle_plaquette(io, oracle, tmp_path):
     assert oracle.plaquette(list(L_MIXED), V) == oracle.plaquette(list(L_MIXED), U)
 
 
+def test_bridge_text_round_trip_and_layout(oracle, tmp_path):
+    """Bridge++ text (bridge_format.jl:201-297): one real per line, sites with
+    x fastest, then direction, row, column, real before imaginary."""
+    entry.load_package()
+    from gaugefields_gb300 import bridge
+    U = _links(oracle, L_MIXED, 12)
+    f = tmp_path / "conf.txt"
+    bridge.write(str(f), U, L_MIXED)
+    lines = f.read_text().split("\n")[:-1]
+    V = int(np.prod(L_MIXED))
+    assert len(lines) == 4 * 9 * 2 * V
+    NX, NY, NZ, NT = L_MIXED
+    x, y, z, t, mu, row, col = 3, 1, 5, 1, 2, 0, 2
+    lex = x + NX * (y + NY * (z + NZ * t))
+    k = (((lex * 4 + mu) * 3 + row) * 3 + col) * 2
+    assert float(lines[k]) == U[mu, lex, col, row].real and float(lines[k + 1]) == U[mu, lex, col, row].imag
+    assert np.array_equal(bridge.read(str(f), L_MIXED), U)
+    # the notation Julia's println uses reads back too
+    g = tmp_path / "julia.txt"
+    g.write_text("\n".join(("%.17e" % float(v)).replace("e-0", "e-").replace("e+0", "e") for v in lines) + "\n")
+    assert np.array_equal(bridge.read(str(g), L_MIXED), U)
+    with pytest.raises(ValueError):
+        bridge.read(str(f), (4, 4, 4, 4))         # line count of another lattice
+
+
 def test_package_exports_the_configuration_io(pkg):
     assert callable(pkg.save_configuration) and callable(pkg.load_configuration_)
     with pytest.raises(ValueError):
-        pkg.save_configuration("x.ildg", None, format="bridge")
+        pkg.save_configuration("x.ildg", None, format="jld2")
     with pytest.raises(ValueError):
         pkg.load_configuration_(None, "x.ildg", format="jld2")
 
@@ -158,3 +184,8 @@ def test_save_and_load_through_the_device(pkg, tmp_path):
         pkg.load_configuration_(pkg.gauge_configuration(L4, start="cold"), f, format="ildg")
     with pytest.raises(ValueError):
         pkg.save_configuration(f, U, format="jld2")
+    t = str(tmp_path / "dev.txt")
+    pkg.save_configuration(t, U, format="bridge")
+    X = pkg.gauge_configuration(L_MIXED, start="cold")
+    pkg.load_configuration_(X, t, format="bridge")
+    assert np.array_equal(X.to_host(), U.to_host())
