@@ -163,3 +163,25 @@ def test_hamiltonian_with_alternating_level_buffers(pkg, nlev):
     h = {prec: pkg.md_hamiltonian(U, P, _driver(pkg, U, 6.0, prec, rho=rho)) for prec in ("fp64", "mixed", "dfloat")}
     assert abs(h["mixed"] - h["fp64"]) <= 1e-13 * abs(h["fp64"])
     assert abs(h["dfloat"] - h["fp64"]) <= 1e-13 * abs(h["fp64"])
+
+
+def test_partial_blocks_in_every_form(pkg, oracle, exact_exp_oracle):
+    """A 6x4x4x6 lattice (576 sites, not a multiple of the 128-thread blocks):
+    the stout force of every form and a double-float trajectory against the
+    oracle, so that the idle threads of the last block of each kernel are
+    exercised."""
+    L = (6, 4, 4, 6)
+    U = pkg.gauge_configuration(L, start="hot", seed=23)
+    Uh = U.to_host()
+    ref = oracle.stout_force(list(L), Uh, [0.1, 0.1], 6.0)
+    for prec, tol in (("fp64", 1e-11), ("dfloat", 1e-11), ("mixed", 1e-4)):
+        P = pkg.gauge_momenta(U)
+        pkg.update_momenta_(P, U, 1.0, _driver(pkg, U, 6.0, prec))
+        assert frob_mom(P.to_host(), ref) < tol * max(1.0, np.abs(ref).max()), prec
+    P = pkg.gaussian_momenta(U, seed=24)
+    Ph = P.to_host()
+    res = pkg.md_trajectory_(U, P, _driver(pkg, U, 6.0, "dfloat", rho=(0.1,), steps=3, trajectory_length=0.3,
+                                           reunitarize=False))
+    h = exact_exp_oracle.md_trajectory(list(L), Uh, Ph, 6.0, 0.3, 3, rho=[0.1])
+    assert abs(res.delta_hamiltonian - h[2]) <= 1e-10
+    assert frob_links(U.to_host(), Uh) < 1e-12
