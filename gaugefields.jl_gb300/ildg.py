@@ -16,9 +16,11 @@ records, as the reference writes it through lime_pack
   imaginary (ildg_format.jl:697-745, :862-887).
 
 A file may hold several configurations; reading takes the one at `index`
-(the reference's ildg[i], ildg_format.jl:902). The reference reads the
-precision from the header and assumes 32 when the element is missing
-(ildg_format.jl:1111); so does this reader.
+(the reference's ildg[i], ildg_format.jl:902). The header rules follow the
+reference's reader: the precision comes from the header, 32 when no header
+has given one (ildg_format.jl:1111), and a binary record without any header
+record, as in the reference's own test files, is read at precision 64 on
+the caller's lattice (ildg_format.jl:917-921).
 
 The functions here work on host arrays in this package's host layout, the
 reference's per-direction (3, 3, NX, NY, NZ, NT) arrays: a complex128 array of
@@ -106,29 +108,48 @@ def _xml_int(xml, tag):
 
 def headers(path):
     """The configurations of an ILDG file: for each ildg-binary-data record,
-    the lattice, colours and precision of the ildg-format record before it
-    and the record's place (extract_info_fromdict, ildg_format.jl:1100-1206)."""
+    the lattice, colours and precision of the last header record before it
+    and the record's place (extract_info_fromdict, ildg_format.jl:1100-1206).
+
+    As in the reference, a header record is either "ildg-format" (lx..lt,
+    field, precision) or "scidac-private-file-xml" (dims); the colour count
+    and the precision carry over from one header record to the next, starting
+    at 3 and 32, so an ildg-format record without a precision element has the
+    previous one's; a binary record after another one keeps the header of the
+    first. A binary record with no header record before it has L, NC and
+    precision None: the reader then takes the caller's lattice and colours and
+    precision 64, as load_gaugefield! does (ildg_format.jl:917-921)."""
     recs = read_records(path)
     out, fmt = [], None
+    nc, precision = 3, 32
     with open(path, "rb") as fp:
         for r in recs:
-            if r["type"] == "ildg-format":
+            if r["type"] in ("ildg-format", "scidac-private-file-xml"):
                 fp.seek(r["offset"])
                 xml = fp.read(r["length"]).decode(errors="replace")
-                dims = [_xml_int(xml, t) for t in ("lx", "ly", "lz", "lt")]
-                if None in dims:
-                    raise ValueError("%s: ildg-format record without lx, ly, lz, lt" % path)
-                prec = _xml_int(xml, "precision")
-                field = re.search(r"<field>\s*su(\d+)gauge\s*</field>", xml)
-                fmt = {"L": tuple(int(d) for d in dims), "NC": int(field.group(1)) if field else 3,
-                       "precision": int(prec) if prec is not None else 32}
+                if r["type"] == "ildg-format":
+                    dims = [_xml_int(xml, t) for t in ("lx", "ly", "lz", "lt")]
+                    if None in dims:
+                        raise ValueError("%s: ildg-format record without lx, ly, lz, lt" % path)
+                    field = re.search(r"<field>\s*([^<\s]+)\s*</field>", xml)
+                    if field:
+                        m = re.fullmatch(r"su(\d+)gauge", field.group(1))
+                        if not m:
+                            raise ValueError("%s: field %r is not an su(N) gauge field" % (path, field.group(1)))
+                        nc = int(m.group(1))
+                    prec = _xml_int(xml, "precision")
+                    if prec is not None:
+                        precision = int(prec)
+                else:
+                    m = re.search(r"<dims>\s*([^<]*?)\s*</dims>", xml)
+                    dims = m.group(1).split() if m else []
+                    if len(dims) != 4:
+                        raise ValueError("%s: scidac-private-file-xml record without four dims" % path)
+                fmt = {"L": tuple(int(d) for d in dims), "NC": nc, "precision": precision}
             elif r["type"] == "ildg-binary-data":
-                if fmt is None:
-                    raise ValueError("%s: ildg-binary-data record %d.%d without an ildg-format record before it"
-                                     % (path, r["message"], r["record"]))
-                out.append(dict(fmt, message=r["message"], record=r["record"], offset=r["offset"],
+                head = fmt if fmt is not None else {"L": None, "NC": None, "precision": None}
+                out.append(dict(head, message=r["message"], record=r["record"], offset=r["offset"],
                                 length=r["length"]))
-                fmt = None
     return out
 
 
@@ -153,27 +174,39 @@ def write(path, links, L, precision=64, append=False):
         write_records(fp, [("ildg-format", format_xml(L, precision).encode()), ("ildg-binary-data", payload)])
 
 
-def read(path, L=None, index=1):
-    """Read configuration `index` (1-based) into the host layout; checks the
-    lattice against L when given. Returns (links, header)."""
+def read(path, L=None, index=1, NC=3):
+    """Read configuration `index` (1-based) into the host layout, a complex
+    array of shape (4, V, NC, NC); checks the lattice against L and the colour
+    count against NC. L is required when the binary record has no header
+    record before it. Returns (links, header) with the header's L, NC and
+    precision filled in. The backend's fields take NC = 3; other NC serve
+    reading the reference's SU(2) files."""
     hs = headers(path)
     if not hs:
         raise ValueError("%s: no ildg-binary-data record" % path)
     if not 1 <= index <= len(hs):
         raise ValueError("%s holds %d configuration(s); index %d" % (path, len(hs), index))
-    h = hs[index - 1]
-    if h["NC"] != 3:
-        raise ValueError("%s: su(%d) field; this backend holds SU(3) links" % (path, h["NC"]))
+    h = dict(hs[index - 1])
+    if h["L"] is None:
+        if L is None:
+            raise ValueError("%s: binary record %d.%d has no header record; the lattice must be given"
+                             % (path, h["message"], h["record"]))
+        h.update(L=tuple(int(x) for x in L), NC=int(NC), precision=64)
+    if h["NC"] != NC:
+        raise ValueError("%s: su(%d) field; expected su(%d)" % (path, h["NC"], NC))
     if L is not None and tuple(int(x) for x in L) != h["L"]:
         raise ValueError("%s: lattice %s does not match the target %s" % (path, h["L"], tuple(L)))
+    if h["precision"] not in (32, 64):
+        raise ValueError("%s: ILDG precision must be 32 or 64, got %r" % (path, h["precision"]))
     V = int(np.prod(h["L"]))
     width = 8 if h["precision"] == 64 else 4
-    if h["length"] != V * 4 * 9 * 2 * width:
-        raise ValueError("%s: binary record of %d bytes; a %s lattice at precision %d needs %d"
-                         % (path, h["length"], h["L"], h["precision"], V * 4 * 9 * 2 * width))
+    need = V * 4 * NC * NC * 2 * width
+    if h["length"] != need:
+        raise ValueError("%s: binary record of %d bytes; a %s su(%d) lattice at precision %d needs %d"
+                         % (path, h["length"], h["L"], NC, h["precision"], need))
     with open(path, "rb") as fp:
         fp.seek(h["offset"])
         raw = np.frombuffer(fp.read(h["length"]), dtype=">f8" if width == 8 else ">f4")
-    ordered = raw.astype(np.float64).view(np.complex128).reshape(V, 4, 3, 3)   # [lex, mu, row, col]
+    ordered = raw.astype(np.float64).view(np.complex128).reshape(V, 4, NC, NC)   # [lex, mu, row, col]
     links = np.ascontiguousarray(np.swapaxes(np.transpose(ordered, (1, 0, 2, 3)), -1, -2))
     return links, h

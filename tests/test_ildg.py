@@ -106,6 +106,96 @@ def test_missing_precision_element_means_32(io, oracle, tmp_path):
     assert h["precision"] == 32 and np.abs(V - U).max() < 1.2e-7
 
 
+def test_header_rules_of_the_reference_reader(io, oracle, tmp_path):
+    """extract_info_fromdict (ildg_format.jl:1100-1206): the precision carries
+    over between header records; a second binary record keeps the header of
+    the first; a scidac-private-file-xml record gives the lattice; a binary
+    record with no header is read at precision 64 on the caller's lattice
+    (load_gaugefield!, ildg_format.jl:917-921)."""
+    A, B = _links(oracle, L4, 13), _links(oracle, L4, 14)
+
+    def payload(U, dt):
+        ordered = np.ascontiguousarray(np.transpose(np.swapaxes(U, -1, -2), (1, 0, 2, 3)))
+        return ordered.view(np.float64).reshape(-1).astype(dt).tobytes()
+
+    f = tmp_path / "carry.ildg"
+    no_prec = io.format_xml(L4, 64).replace("  <precision>64</precision>\n", "").encode()
+    with open(f, "wb") as fp:
+        io.write_records(fp, [("ildg-format", io.format_xml(L4, 64).encode()), ("ildg-binary-data", payload(A, ">f8"))])
+        io.write_records(fp, [("ildg-format", no_prec), ("ildg-binary-data", payload(B, ">f8")),
+                              ("ildg-binary-data", payload(A, ">f8"))])
+    hs = io.headers(str(f))
+    assert [h["precision"] for h in hs] == [64, 64, 64] and [h["message"] for h in hs] == [1, 2, 2]
+    assert np.array_equal(io.read(str(f), index=2)[0], B) and np.array_equal(io.read(str(f), index=3)[0], A)
+
+    g = tmp_path / "scidac.ildg"
+    scidac = b"<?xml version=\"1.0\"?><scidacFile><version>1.1</version><spacetime>4</spacetime>" \
+             b"<dims>4 4 4 4 </dims><volfmt>0</volfmt></scidacFile>"
+    with open(g, "wb") as fp:
+        io.write_records(fp, [("scidac-private-file-xml", scidac), ("ildg-binary-data", payload(A, ">f4"))])
+    V, h = io.read(str(g), L=L4)
+    assert h["L"] == L4 and h["precision"] == 32 and np.abs(V - A).max() < 1.2e-7
+
+    n = tmp_path / "bare.ildg"
+    with open(n, "wb") as fp:
+        io.write_records(fp, [("ildg-binary-data", payload(B, ">f8"))])
+    assert io.headers(str(n))[0]["L"] is None
+    with pytest.raises(ValueError):
+        io.read(str(n))                            # no header and no lattice
+    V, h = io.read(str(n), L=L4)
+    assert np.array_equal(V, B) and h["precision"] == 64 and h["L"] == L4 and h["NC"] == 3
+    with pytest.raises(ValueError):
+        io.read(str(n), L=(4, 4, 4, 2))            # payload size of another lattice
+
+
+def _pin():
+    import importlib.util
+    import os
+    spec = importlib.util.spec_from_file_location(
+        "ildg_reference_pin", os.path.join(os.path.dirname(__file__), "golden", "ildg_reference_pin.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_reference_ildg_files_pin_the_payload_order(io):
+    """The reference's own SU(2) test file has the plaquette that its test
+    set expects (test/init.jl:407-425) in the reader's payload order and not
+    with the matrices transposed. The record was made by
+    tests/golden/ildg_reference_pin.py; where the reference tree is present,
+    the files are read again and must give the recorded numbers bit for bit."""
+    import json
+    import os
+    pin = _pin()
+    with open(pin.RECORD) as fp:
+        record = json.load(fp)["reference_files"]
+    assert set(record) == set(pin.FIXTURES)
+    pinned = 0
+    for name, e in record.items():
+        assert e["precision"] == 64 and [r["type"] for r in e["records"]] == ["ildg-binary-data"]
+        assert e["max_unitarity_error"] < 1e-14
+        if e["golden_plaquette"] is not None:
+            g = e["golden_plaquette"]
+            assert abs(e["plaquette"] - g) <= 1e-13 * abs(g) and abs(e["plaquette"] - g) <= e["golden_rtol"] * abs(g)
+            assert abs(e["plaquette_transposed"] - g) > 0.5 * abs(g)
+            pinned += 1
+    assert pinned == 1
+    root = pin.reference_root()
+    present = [n for n in record if os.path.exists(os.path.join(root, n))]
+    if not present:
+        pytest.skip("reference test files not present; checked the record only")
+    for name in present:
+        again = pin.derive(root, name, pin.FIXTURES[name], io)
+        for key in ("sha256", "bytes", "records", "precision", "plaquette", "plaquette_transposed"):
+            assert again[key] == record[name][key], (name, key)
+
+
+def test_su2_plaquette_helper_on_a_cold_field():
+    pin = _pin()
+    cold = np.broadcast_to(np.eye(2, dtype=np.complex128), (4, 4 ** 4, 2, 2))
+    assert pin.plaquette(cold, (4, 4, 4, 4), 2) == 1.0
+
+
 def test_rejections(io, oracle, tmp_path):
     U = _links(oracle, L4, 10)
     f = tmp_path / "g.ildg"
