@@ -27,7 +27,7 @@ __all__ = [
     "md_action_workspace", "update_gaugefields_", "update_momenta_", "md_step_", "md_trajectory_",
     "hmc_update_", "STOUT_Layer", "CovNeuralnet", "stout_smearing", "smear", "calc_smearedU", "back_prop",
     "Gradientflow", "gradient_flow", "flow_", "add_force_", "energy_density_plaquette", "substitute_U_",
-    "similar", "clear_U_", "save_configuration", "load_configuration_",
+    "similar", "clear_U_", "save_configuration", "load_configuration_", "Oneinstanton_SUN_embedded",
 ]
 
 
@@ -223,6 +223,25 @@ def gauge_configuration(lattice, backend=None, colors=3, halo=1, start="cold", s
             seed = int.from_bytes(os.urandom(8), "little")
         call("gf_hot_start", ctx.h, U.field.h, ctypes.c_uint64(int(seed)), ctx=ctx.h)
     return U
+
+
+def Oneinstanton_SUN_embedded(NC, NX, NY, NZ, NT, NDW=0, center=None, radius=None, sign=1, block=(1, 2),
+                              backend=None):
+    """Oneinstanton_SUN_embedded(NC, NX, NY, NZ, NT; center, radius, sign, block)
+    (src/AbstractGaugefields.jl:1495-1581): the lattice SU(2) instanton placed
+    in the colour rows and columns `block` of SU(3) links. The links are built
+    on the host (special.py) and uploaded, as the reference builds them on the
+    host before copying them to its lattice (its default centre L/2 + 1/2 and
+    radius NX div 2)."""
+    from . import special
+    if NC != 3:
+        raise ValueError("the GB300 backend implements SU(3) only; got NC=%d" % NC)
+    if not isinstance(NDW, (int, np.integer)) or NDW < 0:
+        raise ValueError("NDW must be a nonnegative integer; got %r" % (NDW,))
+    L = (NX, NY, NZ, NT)
+    links = special.oneinstanton_sun_embedded(NC, L, center=center, radius=radius, sign=sign, block=block)
+    U = gauge_configuration(L, backend=backend, start="cold")
+    return U.from_host(links)
 
 
 # ---------------------------------------------------------------------------
