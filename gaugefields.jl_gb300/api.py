@@ -28,6 +28,7 @@ __all__ = [
     "hmc_update_", "STOUT_Layer", "CovNeuralnet", "stout_smearing", "smear", "calc_smearedU", "back_prop",
     "Gradientflow", "gradient_flow", "flow_", "add_force_", "energy_density_plaquette", "substitute_U_",
     "similar", "clear_U_", "save_configuration", "load_configuration_", "Oneinstanton_SUN_embedded",
+    "MDActionSet", "MDForceGroup", "SextonWeingarten",
 ]
 
 
@@ -412,6 +413,99 @@ class OmelyanPQP:
         self.lam = float(lam)
 
 
+class MDActionSet:
+    """MDActionSet(; name=action, ...) (molecular_dynamics.jl:45-66): named
+    action providers whose potentials and forces add. On this backend the
+    members are Wilson plaquette actions on the driver's (possibly smeared)
+    links. Their forces are linear in the couplings, so the force of any
+    group of members is the force of one Wilson action with the group's
+    summed beta: a group's momentum update is one fused force pass."""
+
+    def __init__(self, terms=None, **named):
+        terms = dict(terms or {}, **named)
+        if not terms:
+            raise ValueError("an MDActionSet must contain at least one action provider")
+        for name, a in terms.items():
+            if not isinstance(a, GaugeAction) or not a.terms:
+                raise ValueError("md_action_workspace is not implemented for %s (member %s)"
+                                 % (type(a).__name__, name))
+        self.terms = terms
+
+    @property
+    def beta(self):
+        return sum(a.beta for a in self.terms.values())
+
+    def group_beta(self, group):
+        unknown = [n for n in group.names if n not in self.terms]
+        if unknown:
+            raise ValueError("the force group selects unknown actions %s; available names are %s"
+                             % (tuple(unknown), tuple(self.terms)))
+        return sum(self.terms[n].beta for n in group.names)
+
+
+class MDForceGroup:
+    """MDForceGroup(names...) (molecular_dynamics.jl:68-93): the members of an
+    MDActionSet that one momentum update applies."""
+
+    def __init__(self, *names):
+        if len(names) == 1 and isinstance(names[0], (tuple, list)):
+            names = tuple(names[0])
+        if not names:
+            raise ValueError("an MDForceGroup must contain at least one action name")
+        if len(set(names)) != len(names):
+            raise ValueError("an MDForceGroup must not contain duplicate action names: %s" % (names,))
+        self.names = tuple(str(n) for n in names)
+
+
+def _force_group(group):
+    if isinstance(group, MDForceGroup):
+        return group
+    if isinstance(group, str):
+        return MDForceGroup(group)
+    if isinstance(group, (tuple, list)):
+        return MDForceGroup(*group)
+    raise ValueError("a force group is an action name, a tuple of names or an MDForceGroup; got %r" % (group,))
+
+
+class SextonWeingarten:
+    """SextonWeingarten(; slow, fast, n_fast, ordering=QPQ())
+    (molecular_dynamics.jl:296-360): two force time scales. QPQ ordering: a
+    half-duration fast evolution of n_fast QPQ substeps on each side of one
+    full slow kick; PQP ordering: half slow kicks around one full-duration
+    fast evolution (molecular_dynamics.jl:618-686). The steps run from the
+    host through update_momenta_ and update_gaugefields_."""
+
+    def __init__(self, *, slow, fast, n_fast, ordering=None):
+        ordering = QPQ() if ordering is None else ordering
+        if isinstance(n_fast, bool) or int(n_fast) != n_fast or n_fast <= 0:
+            raise ValueError("n_fast must be positive; got %s" % (n_fast,))
+        if not isinstance(ordering, (QPQ, PQP)):
+            raise ValueError("SextonWeingarten ordering must be PQP() or QPQ(); got %s" % type(ordering).__name__)
+        self.slow = _force_group(slow)
+        self.fast = _force_group(fast)
+        self.n_fast = int(n_fast)
+        self.ordering = ordering
+
+
+def _validate_integrator(integrator, action):
+    """_validate_md_integrator (molecular_dynamics.jl:364-402)."""
+    if not isinstance(integrator, SextonWeingarten):
+        return
+    if not isinstance(action, MDActionSet):
+        raise ValueError("SextonWeingarten requires an MDActionSet; got %s" % type(action).__name__)
+    slow, fast = integrator.slow.names, integrator.fast.names
+    overlap = [n for n in slow if n in fast]
+    if overlap:
+        raise ValueError("slow and fast force groups overlap: %s" % (tuple(overlap),))
+    unknown = [n for n in slow + fast if n not in action.terms]
+    if unknown:
+        raise ValueError("SextonWeingarten selects unknown actions %s; available names are %s"
+                         % (tuple(unknown), tuple(action.terms)))
+    omitted = [n for n in action.terms if n not in slow + fast]
+    if omitted:
+        raise ValueError("SextonWeingarten does not schedule actions %s" % (tuple(omitted),))
+
+
 _PRECISION = {"fp64": _lib.GF_FP64, "mixed": _lib.GF_MIXED, "dfloat": _lib.GF_DFLOAT}
 
 
@@ -427,9 +521,17 @@ class MDDriver:
         self.reunitarize = reunitarize
         self.recompute = recompute
 
-    def params(self):
+    def params(self, group=None):
+        """The gf_md_params of this driver; with a force group, beta is the
+        group's summed coupling."""
         p = MDParams()
-        p.beta = self.action.beta
+        if group is None:
+            p.beta = self.action.beta
+        else:
+            if not isinstance(self.action, MDActionSet):
+                raise ValueError("a force group selects members of an MDActionSet; the driver holds a %s"
+                                 % type(self.action).__name__)
+            p.beta = self.action.group_beta(_force_group(group))
         p.tau = self.trajectory_length
         p.steps = self.steps
         if isinstance(self.integrator, OmelyanPQP):
@@ -470,10 +572,11 @@ def md_driver(U, action, steps, trajectory_length=1.0, integrator=None, smearing
         raise ValueError("trajectory_length must not be zero")
     if precision not in _PRECISION:
         raise ValueError("precision must be 'fp64', 'mixed' or 'dfloat'")
-    if not (isinstance(integrator, (QPQ, PQP, OmelyanPQP)) or callable(integrator)):
+    if not (isinstance(integrator, (QPQ, PQP, OmelyanPQP, SextonWeingarten)) or callable(integrator)):
         raise ValueError("md_step! is not implemented for %s" % type(integrator).__name__)
-    if not isinstance(action, GaugeAction) or not action.terms:
+    if not (isinstance(action, MDActionSet) or (isinstance(action, GaugeAction) and action.terms)):
         raise ValueError("md_action_workspace is not implemented for %s" % type(action).__name__)
+    _validate_integrator(integrator, action)
     return MDDriver(action, integrator, float(trajectory_length), int(steps), smearing, precision, reunitarize,
                     recompute)
 
@@ -495,9 +598,17 @@ def md_potential(action, U, workspace=None, smearing=None):
     return out.value
 
 
-def md_force_(force, action, U, workspace=None):
-    """md_force!(F, ::GaugeAction, U, ws) (molecular_dynamics.jl:251-267)."""
-    call("gf_force", U.ctx.h, U.field.h, ctypes.c_double(action.beta), force.field.h, ctx=U.ctx.h)
+def md_force_(force, action, U, workspace=None, group=None):
+    """md_force!(F, ::GaugeAction, U, ws) (molecular_dynamics.jl:251-267); for
+    an MDActionSet the sum of its members' forces, or of a group's
+    (molecular_dynamics.jl:200-236)."""
+    if group is not None:
+        if not isinstance(action, MDActionSet):
+            raise ValueError("a force group selects members of an MDActionSet; got %s" % type(action).__name__)
+        beta = action.group_beta(_force_group(group))
+    else:
+        beta = action.beta
+    call("gf_force", U.ctx.h, U.field.h, ctypes.c_double(beta), force.field.h, ctx=U.ctx.h)
     return None
 
 
@@ -520,12 +631,13 @@ def update_gaugefields_(U, P, step_size, driver):
     return U
 
 
-def update_momenta_(P, U, step_size, driver):
+def update_momenta_(P, U, step_size, driver, group=None):
     """P <- P + step_size * F(U) (molecular_dynamics.jl:539-551) with the
-    driver's action, smearing and precision."""
+    driver's action, smearing and precision; with a force group, only the
+    selected members of the driver's MDActionSet (molecular_dynamics.jl:553-584)."""
     if not math.isfinite(step_size):
         raise ValueError("the momentum step size must be finite; got %s" % step_size)
-    p = driver.params()
+    p = driver.params(group)
     call("gf_md_mom_update", U.ctx.h, P.field.h, U.field.h, ctypes.c_double(step_size), ctypes.byref(p),
          ctx=U.ctx.h)
     return P
@@ -550,10 +662,34 @@ def md_step_(integrator, U, P, step_size, driver):
         update_gaugefields_(U, P, step_size / 2, driver)
         update_momenta_(P, U, step_size, driver)
         update_gaugefields_(U, P, step_size / 2, driver)
+    elif isinstance(integrator, SextonWeingarten):
+        _sexton_weingarten_step(integrator, U, P, step_size, driver)
     elif callable(integrator):
         integrator(U, P, step_size, driver)
     else:
         raise ValueError("md_step! is not implemented for %s" % type(integrator).__name__)
+
+
+def _fast_evolution(U, P, duration, n, driver, fast):
+    """n QPQ substeps of the fast group over `duration`, the half link steps
+    between substeps applied as one (_md_fast_qpq!, molecular_dynamics.jl:618-633)."""
+    h = duration / n
+    update_gaugefields_(U, P, h / 2, driver)
+    for i in range(n):
+        update_momenta_(P, U, h, driver, fast)
+        update_gaugefields_(U, P, h if i < n - 1 else h / 2, driver)
+
+
+def _sexton_weingarten_step(sw, U, P, step_size, driver):
+    """One Sexton-Weingarten step (molecular_dynamics.jl:635-686)."""
+    if isinstance(sw.ordering, QPQ):
+        _fast_evolution(U, P, step_size / 2, sw.n_fast, driver, sw.fast)
+        update_momenta_(P, U, step_size, driver, sw.slow)
+        _fast_evolution(U, P, step_size / 2, sw.n_fast, driver, sw.fast)
+    else:
+        update_momenta_(P, U, step_size / 2, driver, sw.slow)
+        _fast_evolution(U, P, step_size, sw.n_fast, driver, sw.fast)
+        update_momenta_(P, U, step_size / 2, driver, sw.slow)
 
 
 MDResult = namedtuple("MDResult", ["initial_hamiltonian", "final_hamiltonian", "delta_hamiltonian"])
@@ -561,7 +697,9 @@ MDResult = namedtuple("MDResult", ["initial_hamiltonian", "final_hamiltonian", "
 
 def md_trajectory_(U, P, driver, diagnostics=True):
     """md_trajectory!(U, P, driver) (molecular_dynamics.jl:712-730). The builtin
-    QPQ/PQP run as one native call; custom integrators step from Python."""
+    QPQ/PQP/Omelyan run as one native call; SextonWeingarten and custom
+    integrators step from the host through update_momenta_ and
+    update_gaugefields_."""
     if isinstance(driver.integrator, (QPQ, PQP, OmelyanPQP)):
         p = driver.params()
         out = (ctypes.c_double * 3)()
@@ -584,7 +722,8 @@ def hmc_update_(U, P, driver, seed, sweep, unif):
     """Momentum refresh + md_trajectory! + Metropolis (docs/src/hmc.md:22-81);
     a rejected trajectory restores U."""
     if not isinstance(driver.integrator, (QPQ, PQP, OmelyanPQP)):
-        raise ValueError("hmc_update_ runs the builtin integrators natively")
+        raise ValueError("hmc_update_ runs the builtin integrators natively; for %s use gaussian_momenta_, "
+                         "md_trajectory_ and the Metropolis test on the host" % type(driver.integrator).__name__)
     p = driver.params()
     out = (ctypes.c_double * 4)()
     call("gf_hmc_update", U.ctx.h, U.field.h, P.field.h, ctypes.byref(p), ctypes.c_uint64(int(seed)),
