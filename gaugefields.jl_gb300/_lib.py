@@ -46,6 +46,7 @@ class MDParams(ctypes.Structure):
         ("reunitarize", ctypes.c_int),
         ("stout_recompute", ctypes.c_int),
         ("lam", ctypes.c_double),
+        ("c_rect", ctypes.c_double),
     ]
 
 
@@ -79,9 +80,12 @@ SIGNATURES = {
     "gf_reunitarize": [_P, _P],
     "gf_plaquette": [_P, _P, _DP],
     "gf_action": [_P, _P, _D, _DP],
+    "gf_rectangle": [_P, _P, _DP],
+    "gf_action_loops": [_P, _P, _D, _D, _DP],
     "gf_kinetic": [_P, _P, _DP],
     "gf_staple": [_P, _P, _I, _P],
     "gf_force": [_P, _P, _D, _P],
+    "gf_force_loops": [_P, _P, _D, _D, _P],
     "gf_mom_update": [_P, _P, _P, _D, _D],
     "gf_link_update": [_P, _P, _P, _D, _I],
     "gf_hamiltonian": [_P, _P, _P, ctypes.POINTER(MDParams), _DP],
@@ -104,12 +108,13 @@ SIGNATURES = {
 
 KERNEL_CLASSES = ["plaquette", "force", "link_update", "stout_fwd", "bwd_local", "bwd_gather", "stout_fwd64",
                   "bwd_local64", "bwd_gather64", "other", "link_update_df", "stout_fwd_df", "force_df",
-                  "bwd_local_df", "bwd_gather_df"]
+                  "bwd_local_df", "bwd_gather_df", "rect"]
 # arithmetic precision of each class (the force class follows its links)
 KERNEL_PRECISION = {"plaquette": "fp64", "force": "fp32", "link_update": "fp64", "stout_fwd": "fp32",
                     "bwd_local": "fp32", "bwd_gather": "fp32", "stout_fwd64": "fp64", "bwd_local64": "fp64",
                     "bwd_gather64": "fp64", "other": "fp64", "link_update_df": "df", "stout_fwd_df": "df",
-                    "force_df": "df", "bwd_local_df": "df", "bwd_gather_df": "df"}
+                    "force_df": "df", "bwd_local_df": "df", "bwd_gather_df": "df",
+                    "rect": "fp64"}
 
 _lib = None
 

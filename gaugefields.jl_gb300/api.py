@@ -28,7 +28,7 @@ __all__ = [
     "hmc_update_", "STOUT_Layer", "CovNeuralnet", "stout_smearing", "smear", "calc_smearedU", "back_prop",
     "Gradientflow", "gradient_flow", "flow_", "add_force_", "energy_density_plaquette", "substitute_U_",
     "similar", "clear_U_", "save_configuration", "load_configuration_", "Oneinstanton_SUN_embedded",
-    "MDActionSet", "MDForceGroup", "SextonWeingarten",
+    "MDActionSet", "MDForceGroup", "SextonWeingarten", "rectangle_sum",
 ]
 
 
@@ -361,9 +361,16 @@ def gaussian_momenta(U, sigma=1.0, seed=None, sweep=0):
 # ---------------------------------------------------------------------------
 # gauge action (src/action/GaugeActions.jl)
 # ---------------------------------------------------------------------------
+_LOOPS = {"plaquette": "plaquette", ("plaquette", "plaquette_dag"): "plaquette",
+          "rectangular": "rectangular", ("rectangular", "rectangular_dag"): "rectangular"}
+
+
 class GaugeAction:
-    """Wilson-loop action. The GB300 backend implements the Wilson plaquette
-    action push!(action, beta/2, plaq U plaq^dag) (docs/src/hmc.md:146-150)."""
+    """Wilson-loop action (src/action/GaugeActions.jl). The GB300 backend
+    implements the plaquette loops push!(action, beta/2, plaq U plaq^dag)
+    (docs/src/hmc.md:146-150) and the rectangle loops push!(action, c,
+    rect U rect^dag) of make_loops_fromname("rectangular") (e.g. Iwasaki or
+    Symanzik improvement, docs/src/legacyapi.md:80-92)."""
 
     def __init__(self, U, hascovnet=False):
         self.terms = []
@@ -371,7 +378,13 @@ class GaugeAction:
 
     @property
     def beta(self):
-        return 2.0 * sum(c for c, _ in self.terms)
+        """Twice the plaquette coefficient (the Wilson beta)."""
+        return 2.0 * sum(c for c, kind in self.terms if kind == "plaquette")
+
+    @property
+    def c_rect(self):
+        """The rectangle coefficient (0 without rectangle loops)."""
+        return sum(c for c, kind in self.terms if kind == "rectangular")
 
 
 def push_(action_or_net, coefficient, loops=None):
@@ -379,17 +392,31 @@ def push_(action_or_net, coefficient, loops=None):
     if isinstance(action_or_net, CovNeuralnet):
         action_or_net.layers.append(coefficient)
         return action_or_net
-    if loops not in ("plaquette", ("plaquette", "plaquette_dag")):
-        raise ValueError("the GB300 backend supports the plaquette loops (with their conjugates) only")
+    kind = _LOOPS.get(loops if not isinstance(loops, list) else tuple(loops))
+    if kind is None:
+        raise ValueError("the GB300 backend supports the plaquette and rectangular loops (with their conjugates); "
+                         "got %r" % (loops,))
     c = float(coefficient.real) if isinstance(coefficient, complex) else float(coefficient)
-    action_or_net.terms.append((c, loops))
+    action_or_net.terms.append((c, kind))
     return action_or_net
+
+
+def rectangle_sum(U):
+    """sum_x sum_{mu<nu} Re tr of the two rectangles (1x2 and 2x1) of the
+    plane at x: the loops of make_rect (src/autostaples/wilsonloops.jl:304-330)."""
+    out = ctypes.c_double()
+    call("gf_rectangle", U.ctx.h, U.field.h, ctypes.byref(out), ctx=U.ctx.h)
+    return out.value
 
 
 def evaluate_GaugeAction(action, U):
     """Traced lattice sum of the action's loops (GaugeActions.jl:132-142):
-    beta/2 * sum tr(plaq + plaq^dag) = beta * sum Re tr P."""
-    return action.beta * calculate_Plaquette(U)
+    beta/2 * sum tr(plaq + plaq^dag) = beta * sum Re tr P, plus
+    c_rect * sum tr(rect + rect^dag) = 2 c_rect * sum Re tr R."""
+    v = action.beta * calculate_Plaquette(U)
+    if action.c_rect != 0.0:
+        v += 2.0 * action.c_rect * rectangle_sum(U)
+    return v
 
 
 # ---------------------------------------------------------------------------
@@ -435,12 +462,22 @@ class MDActionSet:
     def beta(self):
         return sum(a.beta for a in self.terms.values())
 
-    def group_beta(self, group):
+    @property
+    def c_rect(self):
+        return sum(a.c_rect for a in self.terms.values())
+
+    def _members(self, group):
         unknown = [n for n in group.names if n not in self.terms]
         if unknown:
             raise ValueError("the force group selects unknown actions %s; available names are %s"
                              % (tuple(unknown), tuple(self.terms)))
-        return sum(self.terms[n].beta for n in group.names)
+        return [self.terms[n] for n in group.names]
+
+    def group_beta(self, group):
+        return sum(a.beta for a in self._members(group))
+
+    def group_c_rect(self, group):
+        return sum(a.c_rect for a in self._members(group))
 
 
 class MDForceGroup:
@@ -527,11 +564,14 @@ class MDDriver:
         p = MDParams()
         if group is None:
             p.beta = self.action.beta
+            p.c_rect = self.action.c_rect
         else:
             if not isinstance(self.action, MDActionSet):
                 raise ValueError("a force group selects members of an MDActionSet; the driver holds a %s"
                                  % type(self.action).__name__)
-            p.beta = self.action.group_beta(_force_group(group))
+            group = _force_group(group)
+            p.beta = self.action.group_beta(group)
+            p.c_rect = self.action.group_c_rect(group)
         p.tau = self.trajectory_length
         p.steps = self.steps
         if isinstance(self.integrator, OmelyanPQP):
@@ -577,6 +617,9 @@ def md_driver(U, action, steps, trajectory_length=1.0, integrator=None, smearing
     if not (isinstance(action, MDActionSet) or (isinstance(action, GaugeAction) and action.terms)):
         raise ValueError("md_action_workspace is not implemented for %s" % type(action).__name__)
     _validate_integrator(integrator, action)
+    if action.c_rect != 0.0 and (precision != "fp64" or smearing is not None):
+        raise ValueError("the rectangle loops run in the plain fp64 form on thin links (precision 'fp64', "
+                         "no smearing)")
     return MDDriver(action, integrator, float(trajectory_length), int(steps), smearing, precision, reunitarize,
                     recompute)
 
@@ -594,7 +637,11 @@ def md_potential(action, U, workspace=None, smearing=None):
     if smearing is not None:
         U = smear(U, smearing)
     out = ctypes.c_double()
-    call("gf_action", U.ctx.h, U.field.h, ctypes.c_double(action.beta), ctypes.byref(out), ctx=U.ctx.h)
+    if action.c_rect != 0.0:
+        call("gf_action_loops", U.ctx.h, U.field.h, ctypes.c_double(0.5 * action.beta), ctypes.c_double(action.c_rect),
+             ctypes.byref(out), ctx=U.ctx.h)
+    else:
+        call("gf_action", U.ctx.h, U.field.h, ctypes.c_double(action.beta), ctypes.byref(out), ctx=U.ctx.h)
     return out.value
 
 
@@ -605,10 +652,15 @@ def md_force_(force, action, U, workspace=None, group=None):
     if group is not None:
         if not isinstance(action, MDActionSet):
             raise ValueError("a force group selects members of an MDActionSet; got %s" % type(action).__name__)
-        beta = action.group_beta(_force_group(group))
+        group = _force_group(group)
+        beta, c_rect = action.group_beta(group), action.group_c_rect(group)
     else:
-        beta = action.beta
-    call("gf_force", U.ctx.h, U.field.h, ctypes.c_double(beta), force.field.h, ctx=U.ctx.h)
+        beta, c_rect = action.beta, action.c_rect
+    if c_rect != 0.0:
+        call("gf_force_loops", U.ctx.h, U.field.h, ctypes.c_double(0.5 * beta), ctypes.c_double(c_rect),
+             force.field.h, ctx=U.ctx.h)
+    else:
+        call("gf_force", U.ctx.h, U.field.h, ctypes.c_double(beta), force.field.h, ctx=U.ctx.h)
     return None
 
 

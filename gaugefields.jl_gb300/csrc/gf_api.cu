@@ -329,6 +329,25 @@ extern "C" int gf_action(gf_ctx* ctx, const gf_field* U, double beta, double* ou
   *out = -(beta / 3.0) * plaquette_sum(ctx, U);
   API_END(ctx)
 }
+extern "C" int gf_rectangle(gf_ctx* ctx, const gf_field* U, double* out) {
+  API_BEGIN
+  need(ctx && U && out, "gf_rectangle: null argument");
+  need_ctx(ctx, U);
+  need_kind(U, GF_LINK64, "gf_rectangle: U");
+  *out = rectangle_sum(ctx, U);
+  API_END(ctx)
+}
+extern "C" int gf_action_loops(gf_ctx* ctx, const gf_field* U, double c_plaq, double c_rect, double* out) {
+  API_BEGIN
+  need(ctx && U && out, "gf_action_loops: null argument");
+  need_ctx(ctx, U);
+  need(std::isfinite(c_plaq) && std::isfinite(c_rect), "gf_action_loops: the coefficients must be finite");
+  need_kind(U, GF_LINK64, "gf_action_loops: U");
+  double v = c_plaq * plaquette_sum(ctx, U);
+  if (c_rect != 0.0) v += c_rect * rectangle_sum(ctx, U);
+  *out = -(2.0 / 3.0) * v;
+  API_END(ctx)
+}
 extern "C" int gf_kinetic(gf_ctx* ctx, const gf_field* P, double* out) {
   API_BEGIN
   need(ctx && P && out, "gf_kinetic: null argument");
@@ -473,6 +492,9 @@ static void check_md(const gf_md_params* p) {
        "md: precision must be GF_FP64, GF_MIXED or GF_DFLOAT");
   need(p->nstout >= 0 && p->nstout <= GF_MAX_STOUT, "md: nstout must be 0..GF_MAX_STOUT");
   for (int l = 0; l < p->nstout; ++l) need(std::isfinite(p->rho[l]), "md: rho must be finite");
+  need(std::isfinite(p->c_rect), "md: c_rect must be finite");
+  need(p->c_rect == 0.0 || (p->precision == GF_FP64 && p->nstout == 0),
+       "md: the rectangle term runs in the plain fp64 form on thin links (precision GF_FP64, nstout 0)");
 }
 
 // The context's stack for a stack precision. The mixed form's Hamiltonian
@@ -506,6 +528,8 @@ static gf_stout* ctx_stout(gf_ctx* ctx, const gf_md_params* p, int precision) {
 #endif
 static double potential(gf_ctx* ctx, const gf_field* U, const gf_md_params* p) {
   bool df = (GF_DF_HAMILTONIAN && p->precision == GF_MIXED) || p->precision == GF_DFLOAT;
+  if (p->nstout == 0 && p->c_rect != 0.0)
+    return -(p->beta / 3.0) * plaquette_sum(ctx, U) - (2.0 / 3.0) * p->c_rect * rectangle_sum(ctx, U);
   if (p->nstout == 0) return -(p->beta / 3.0) * plaquette_sum(ctx, U);
   gf_stout* st = ctx_stout(ctx, p, df ? GF_PREC_DF : GF_FP64);
   stout_forward(ctx, st, U, nullptr);
@@ -521,6 +545,10 @@ static double hamiltonian(gf_ctx* ctx, const gf_field* U, const gf_field* P, con
 static void mom_update(gf_ctx* ctx, gf_field* P, const gf_field* U, const gf_field* U32, double eps,
                        const gf_md_params* p) {
   const gf_field* links = (p->precision == GF_MIXED) ? U32 : U;
+  if (p->nstout == 0 && p->c_rect != 0.0) {
+    loops_force_coef(ctx, U, P, eps * (-1.0 / 3.0) * (0.5 * p->beta), eps * (-1.0 / 3.0) * p->c_rect, 1.0);
+    return;
+  }
   if (p->nstout == 0) {
     wilson_force_coef(ctx, links, P, eps * (-1.0 / 3.0) * (0.5 * p->beta), 1.0, p->precision == GF_DFLOAT);
     return;
@@ -540,7 +568,8 @@ static void mom_update(gf_ctx* ctx, gf_field* P, const gf_field* U, const gf_fie
 static bool vcache_lookup(const gf_ctx* ctx, const gf_md_params* p, unsigned long long h, double* V) {
   for (int e = 0; e < 2; ++e) {
     const auto& c = ctx->vc[e];
-    if (!c.valid || c.hash != h || c.beta != p->beta || c.nstout != p->nstout || c.precision != p->precision)
+    if (!c.valid || c.hash != h || c.beta != p->beta || c.c_rect != p->c_rect || c.nstout != p->nstout ||
+        c.precision != p->precision)
       continue;
     bool same = true;
     for (int l = 0; l < p->nstout; ++l) same = same && c.rho[l] == p->rho[l];
@@ -564,6 +593,7 @@ static void vcache_set(gf_ctx* ctx, const gf_md_params* p, int e, unsigned long 
   c.hash = h;
   c.V = V;
   c.beta = p->beta;
+  c.c_rect = p->c_rect;
   c.nstout = p->nstout;
   c.precision = p->precision;
   for (int l = 0; l < GF_MAX_STOUT; ++l) c.rho[l] = l < p->nstout ? p->rho[l] : 0.0;
@@ -631,6 +661,17 @@ extern "C" int gf_force(gf_ctx* ctx, const gf_field* U, double beta, gf_field* F
   need_ctx(ctx, F);
   need(std::isfinite(beta), "gf_force: beta must be finite");
   wilson_force_coef(ctx, U, F, -(1.0 / 3.0) * (0.5 * beta), 0.0);
+  API_END(ctx)
+}
+
+extern "C" int gf_force_loops(gf_ctx* ctx, const gf_field* U, double c_plaq, double c_rect, gf_field* F) {
+  API_BEGIN
+  need(ctx && U && F, "gf_force_loops: null argument");
+  need_ctx(ctx, U);
+  need_ctx(ctx, F);
+  need(std::isfinite(c_plaq) && std::isfinite(c_rect), "gf_force_loops: the coefficients must be finite");
+  need_kind(U, GF_LINK64, "gf_force_loops: U");
+  loops_force_coef(ctx, U, F, -(1.0 / 3.0) * c_plaq, -(1.0 / 3.0) * c_rect, 0.0);
   API_END(ctx)
 }
 

@@ -78,7 +78,7 @@ struct gf_ctx {
   struct {
     int valid;
     unsigned long long hash;
-    double V, beta;
+    double V, beta, c_rect;
     int nstout, precision;
     double rho[GF_MAX_STOUT];
   } vc[2];
@@ -160,6 +160,12 @@ void staple_up(gf_ctx* ctx, const gf_field* U, int mu, gf_field* V);  // constru
 // P <- keep * P + coef * TA-coefficients(U_mu * S_mu), S = sum of the six
 // staples (dS/dU order); keep = 0 overwrites P without reading it.
 void wilson_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double coef, double keep, bool df = false);
+
+// ---- rectangle loops (gf_rect.cu) ----
+double rectangle_sum(gf_ctx* ctx, const gf_field* U);  // sum_x sum_{mu<nu} Re tr (R1x2 + R2x1)
+// P <- keep * P + TA-coefficients(U_mu (cp S_mu + cr R_mu)), S the six
+// plaquette staples and R the eighteen rectangle staples of U_mu.
+void loops_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double cp, double cr, double keep);
 
 // ---- link update (gf_update.cu) ----
 // U <- exp(i eps P) U, optional re-unitarisation, optional fp32 shadow copy.

@@ -65,8 +65,9 @@ typedef struct gf_field gf_field;
 typedef struct gf_stout gf_stout;
 
 /* MD parameters: md_driver(U, action; steps, trajectory_length, integrator)
- * (src/molecular_dynamics.jl:440-483) with the Wilson GaugeAction
- * push!(action, beta/2, plaq U plaq^dag) and an optional stout stack
+ * (src/molecular_dynamics.jl:440-483) with the GaugeAction
+ * push!(action, beta/2, plaq U plaq^dag), optionally a rectangle term
+ * push!(action, c_rect, rect U rect^dag), and an optional stout stack
  * (STOUT_Layer, src/smearing/stout_fast.jl:6-121). */
 typedef struct gf_md_params {
   double beta;           /* Wilson coupling */
@@ -81,6 +82,11 @@ typedef struct gf_md_params {
                             stored level input instead of keeping it from the
                             forward pass (less memory, more flops) */
   double lambda;         /* Omelyan parameter (GF_OMELYAN only) */
+  double c_rect;         /* coefficient of the rectangle loops,
+                            push!(action, c_rect, rect U rect') (make_rect,
+                            src/autostaples/wilsonloops.jl:304-330); 0 for the
+                            plain Wilson action. Nonzero needs precision
+                            GF_FP64 and nstout 0 (thin links). */
 } gf_md_params;
 
 /* ---- context ------------------------------------------------------------ */
@@ -147,11 +153,27 @@ int gf_kinetic(gf_ctx* ctx, const gf_field* P, double* out);
  * up staples sum_{nu != mu} U_nu(x) U_mu(x+nu) U_nu(x+mu)^dag into direction
  * slot mu (0-based) of the MAT64/LINK64 field V. */
 int gf_staple(gf_ctx* ctx, const gf_field* U, int mu, gf_field* V);
+/* evaluate_GaugeAction over the rectangle loops of make_rect
+ * (GaugeActions.jl:132-142, wilsonloops.jl:304-330) without the conjugates:
+ * sum_x sum_{mu<nu} Re tr (R^{1x2}_{mu nu}(x) + R^{2x1}_{mu nu}(x)), the loops
+ * (mu,1),(nu,2),(mu,-1),(nu,-2) and (mu,2),(nu,1),(mu,-2),(nu,-1). fp64,
+ * deterministic. */
+int gf_rectangle(gf_ctx* ctx, const gf_field* U, double* out);
+/* md_potential(::GaugeAction) (molecular_dynamics.jl:247) of
+ * push!(action, c_plaq, plaq U plaq') and push!(action, c_rect, rect U rect')
+ * (e.g. Iwasaki: c_plaq = beta (1 - 8 c1)/2, c_rect = beta c1/2, c1 = -0.331):
+ * -(2/3) (c_plaq sum Re tr P + c_rect sum Re tr R). fp64 links (LINK64). */
+int gf_action_loops(gf_ctx* ctx, const gf_field* U, double c_plaq, double c_rect, double* out);
 
 /* ---- molecular dynamics ------------------------------------------------- */
 /* md_force!(F, ::GaugeAction, U, ws) (molecular_dynamics.jl:251-267):
  * F_mu = -(1/3) TA(U_mu dS/dU_mu), dS/dU_mu = beta/2 * sum of six staples. */
 int gf_force(gf_ctx* ctx, const gf_field* U, double beta, gf_field* F);
+/* md_force! of the plaquette + rectangle action of gf_action_loops
+ * (calc_dSdUμ!, GaugeActions.jl:95-123): F_mu = -(1/3) TA(U_mu dS/dU_mu),
+ * dS/dU_mu = c_plaq * (6 plaquette staples) + c_rect * (18 rectangle staples).
+ * fp64, one fused kernel. */
+int gf_force_loops(gf_ctx* ctx, const gf_field* U, double c_plaq, double c_rect, gf_field* F);
 /* update_momenta!(P, U, eps, driver) (molecular_dynamics.jl:539-551):
  * P += eps * F(U), fused in one kernel. */
 int gf_mom_update(gf_ctx* ctx, gf_field* P, const gf_field* U, double eps, double beta);
@@ -242,7 +264,8 @@ int gf_plaquette_noalloc(const void* links, const int L[4], double* out, void* s
 #define GF_K_FORCE_DF 12        /* Wilson staple force in double-float */
 #define GF_K_BWD_LOCAL_DF 13    /* stout adjoint, local part, double-float */
 #define GF_K_BWD_GATHER_DF 14   /* stout adjoint, gather (+ force), double-float */
-#define GF_K_COUNT 15
+#define GF_K_RECT 15            /* rectangle loop sum and plaquette + rectangle force (fp64) */
+#define GF_K_COUNT 16
 /* Enable (on != 0) or disable CUDA-event timing of every kernel launch on the
  * context's stream; enabling clears the accumulators. */
 int gf_prof_enable(gf_ctx* ctx, int on);

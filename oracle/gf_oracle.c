@@ -17,6 +17,7 @@
  *   calc_coefficients_Q                     src/AbstractGaugefields.jl:3284-3344
  *   STOUT forward!/backward + CdexpQdQ!     src/smearing/stout_fast.jl:250-408, 603-785, 888-946, 1031-1081
  *   STOUT_dataset (Cμ, dCμ/dUν lists)       src/smearing/stout_dataset.jl:10-80
+ *   plaquette / rectangle loop sets         src/autostaples/wilsonloops.jl:233-330 (make_plaq, make_rect)
  *   flow! (RK3), add_force!, exp_aF_U!      src/smearing/gradientflow.jl:171-238,
  *                                           src/AbstractGaugefields.jl:2717-2842
  * The Wilson-loop path lists come from the external package Wilsonloop.jl
@@ -655,6 +656,150 @@ void or_force(const int L[4], const cdbl* U, double beta, double* F) {
   free(D);
 }
 
+/* ------------------------------------------------------------------------ */
+/* general loop sets (push!(action, c, loops U loops'))                      */
+/* ------------------------------------------------------------------------ */
+/* A closed loop as unit steps (direction, +-1) from its origin. Kind 0 is the
+ * plaquette set, kind 1 the rectangle set of make_loops_fromname
+ * ("plaquette" / "rectangular"): for mu < nu the loops (mu,1),(nu,1),(mu,-1),
+ * (nu,-1), and (mu,1),(nu,2),(mu,-1),(nu,-2) with (mu,2),(nu,1),(mu,-2),(nu,-1)
+ * (make_plaq / make_rect, src/autostaples/wilsonloops.jl:233-330), each
+ * followed by its Hermitian conjugate (the reversed loop with every step
+ * inverted), as the action's loops U loops' holds it. */
+typedef struct {
+  int n;
+  int st[8][2];
+} Loop;
+
+static void loop_push(Loop* l, int dir, int sign, int count) {
+  for (int i = 0; i < count; ++i) {
+    l->st[l->n][0] = dir;
+    l->st[l->n][1] = sign;
+    l->n++;
+  }
+}
+
+static int loop_set(int kind, Loop* out) {
+  int n = 0;
+  for (int mu = 0; mu < 4; ++mu)
+    for (int nu = mu + 1; nu < 4; ++nu) {
+      const int shapes[2][2] = {{1, 2}, {2, 1}}; /* extent along mu, along nu */
+      const int nshape = kind == 0 ? 1 : 2;
+      for (int k = 0; k < nshape; ++k) {
+        int a = kind == 0 ? 1 : shapes[k][0], b = kind == 0 ? 1 : shapes[k][1];
+        Loop l;
+        l.n = 0;
+        loop_push(&l, mu, +1, a);
+        loop_push(&l, nu, +1, b);
+        loop_push(&l, mu, -1, a);
+        loop_push(&l, nu, -1, b);
+        Loop d;
+        d.n = l.n;
+        for (int i = 0; i < l.n; ++i) {
+          d.st[i][0] = l.st[l.n - 1 - i][0];
+          d.st[i][1] = -l.st[l.n - 1 - i][1];
+        }
+        out[n++] = l;
+        out[n++] = d;
+      }
+    }
+  return n;
+}
+
+/* Staples of a loop set for U_mu (Wilsonloop's make_staple over the set):
+ * every forward occurrence of U_mu in a loop contributes the rest of that
+ * loop, cyclically, as a path starting at x + e_mu. */
+static int loop_staples(int mu, const Loop* loops, int nloops, Path* out) {
+  int n = 0;
+  for (int i = 0; i < nloops; ++i)
+    for (int k = 0; k < loops[i].n; ++k) {
+      if (loops[i].st[k][0] != mu || loops[i].st[k][1] != 1) continue;
+      int rot[8][2];
+      int m = 0;
+      for (int j = 1; j < loops[i].n; ++j) {
+        int q = (k + j) % loops[i].n;
+        rot[m][0] = loops[i].st[q][0];
+        rot[m][1] = loops[i].st[q][1];
+        ++m;
+      }
+      Path p = path_from_steps((const int (*)[2])rot, m);
+      for (int j = 0; j < m; ++j) p.l[j].off[mu] += 1;
+      out[n++] = p;
+    }
+  return n;
+}
+
+/* Re sum_x sum_{loops of the set and their conjugates} tr loop(x) */
+double or_loop_trace(const int L[4], const cdbl* U, int kind) {
+  Lat lat = mklat(L);
+  Loop loops[24];
+  Path paths[24];
+  int nl = loop_set(kind, loops);
+  for (int i = 0; i < nl; ++i) paths[i] = path_from_steps((const int (*)[2])loops[i].st, loops[i].n);
+  double* part = (double*)calloc((size_t)lat.V, sizeof(double));
+#pragma omp parallel for schedule(static)
+  for (long x = 0; x < lat.V; ++x) {
+    cdbl s = 0;
+    for (int i = 0; i < nl; ++i) {
+      M3 a = eval_links(U, &lat, &paths[i], 0, paths[i].n, x);
+      s += mtr(&a);
+    }
+    part[x] = creal(s);
+  }
+  double sum = sum_accurate(part, lat.V);
+  free(part);
+  return sum;
+}
+
+/* md_potential of push!(c_plaq, plaq U plaq'), push!(c_rect, rect U rect'):
+ * -Re(evaluate_GaugeAction)/NC (src/action/GaugeActions.jl:132-142) */
+double or_action_loops(const int L[4], const cdbl* U, double c_plaq, double c_rect) {
+  double v = c_plaq * or_loop_trace(L, U, 0);
+  if (c_rect != 0.0) v += c_rect * or_loop_trace(L, U, 1);
+  return -v / 3.0;
+}
+
+/* md_force! of the same action: F_mu = TA-coefficients of -(1/3) U_mu dS/dU_mu,
+ * dS/dU_mu = sum over the sets of c * (staples of U_mu) (calc_dSdUμ!,
+ * src/action/GaugeActions.jl:95-123) */
+void or_force_loops(const int L[4], const cdbl* U, double c_plaq, double c_rect, double* F) {
+  Lat lat = mklat(L);
+  Loop lp[12], lr[24];
+  int np = loop_set(0, lp), nr = loop_set(1, lr);
+  for (int mu = 0; mu < 4; ++mu) {
+    Path sp[8], sr[32];
+    int nsp = loop_staples(mu, lp, np, sp);
+    int nsr = loop_staples(mu, lr, nr, sr);
+#pragma omp parallel for schedule(static)
+    for (long x = 0; x < lat.V; ++x) {
+      M3 acc = mzero();
+      for (int k = 0; k < nsp; ++k) {
+        M3 t = eval_links(U, &lat, &sp[k], 0, sp[k].n, x);
+        madd(&acc, c_plaq, &t);
+      }
+      if (c_rect != 0.0)
+        for (int k = 0; k < nsr; ++k) {
+          M3 t = eval_links(U, &lat, &sr[k], 0, sr[k].n, x);
+          madd(&acc, c_rect, &t);
+        }
+      M3 u = ld(U, &lat, mu, x);
+      M3 w = mmul(&u, &acc);
+      double* f = F + ((size_t)mu * lat.V + x) * 8;
+      for (int a = 0; a < 8; ++a) f[a] = 0;
+      ta_add(f, -1.0 / 3.0, &w);
+    }
+  }
+}
+
+/* number of staples of U_mu in a set (6 for the plaquettes, 18 for the
+ * rectangles) */
+int or_loop_staple_count(int kind, int mu) {
+  Loop loops[24];
+  Path st[32];
+  int nl = loop_set(kind, loops);
+  return loop_staples(mu, loops, nl, st);
+}
+
 /* add_U!(P, eps, F) over all directions */
 static void mom_axpy(const Lat* lat, double* P, double eps, const double* F) {
   size_t n = (size_t)32 * lat->V;
@@ -927,15 +1072,25 @@ double or_stout_action(const int L[4], const cdbl* U, int nlev, const double* rh
 /* ------------------------------------------------------------------------ */
 /* MD driver                                                                 */
 /* ------------------------------------------------------------------------ */
+/* Coefficient of the rectangle loops rect U rect' in the MD action (0: the
+ * plain Wilson action); with it the action is thin-link. */
+static double g_c_rect = 0.0;
+void or_set_rect(double c_rect) { g_c_rect = c_rect; }
+
 static void mom_update(const int L[4], double* P, const cdbl* U, double eps, double beta, int nstout, const double* rho,
                        double* F) {
   Lat lat = mklat(L);
-  or_stout_force(L, U, nstout, rho, beta, F);
+  if (nstout == 0 && g_c_rect != 0.0)
+    or_force_loops(L, U, 0.5 * beta, g_c_rect, F);
+  else
+    or_stout_force(L, U, nstout, rho, beta, F);
   mom_axpy(&lat, P, eps, F);
 }
 
 double or_hamiltonian(const int L[4], const cdbl* U, const double* P, double beta, int nstout, const double* rho) {
-  return or_stout_action(L, U, nstout, rho, beta) + or_kinetic(L, P) / 2;
+  double v = (nstout == 0 && g_c_rect != 0.0) ? or_action_loops(L, U, 0.5 * beta, g_c_rect)
+                                              : or_stout_action(L, U, nstout, rho, beta);
+  return v + or_kinetic(L, P) / 2;
 }
 
 static double g_omelyan_lambda = 0.1931833275037836;

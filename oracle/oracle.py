@@ -77,6 +77,11 @@ def _declare(l):
         "or_hot_start": ([_P, _P, _U64], None),
         "or_uniform_hot_start": ([_P, _P, _U64], None),
         "or_gauss_mom": ([_P, _P, _U64, _U64], None),
+        "or_loop_trace": ([_P, _P, _I], _D),
+        "or_action_loops": ([_P, _P, _D, _D], _D),
+        "or_force_loops": ([_P, _P, _D, _D, _P], None),
+        "or_loop_staple_count": ([_I, _I], _I),
+        "or_set_rect": ([_D], None),
     }
     for name, (args, res) in sig.items():
         f = getattr(l, name)
@@ -246,21 +251,58 @@ def stout_action(L, U, rho, beta):
     return lib().or_stout_action(_ptr(_L(L)), _ptr(U), len(rho), _ptr(r), float(beta))
 
 
-def hamiltonian(L, U, P, beta, rho=()):
+def hamiltonian(L, U, P, beta, rho=(), c_rect=0.0):
     r = _rho(rho)
-    return lib().or_hamiltonian(_ptr(_L(L)), _ptr(U), _ptr(P), float(beta), len(rho), _ptr(r))
+    lib().or_set_rect(float(c_rect))
+    try:
+        return lib().or_hamiltonian(_ptr(_L(L)), _ptr(U), _ptr(P), float(beta), len(rho), _ptr(r))
+    finally:
+        lib().or_set_rect(0.0)
 
 
-def md_trajectory(L, U, P, beta, tau, steps, integrator="QPQ", rho=(), lam=0.1931833275037836):
-    """In place on U, P. Returns (H0, H1, dH). integrator: QPQ, PQP or OMELYAN."""
+def loop_trace(L, U, kind):
+    """Re sum_x sum tr over the plaquette (kind 0) or rectangle (kind 1) loops
+    and their conjugates: twice the sum of Re tr over the geometric loops."""
+    _chk(U, np.complex128)
+    return lib().or_loop_trace(_ptr(_L(L)), _ptr(U), int(kind))
+
+
+def rectangle_sum(L, U):
+    """sum_x sum_{mu<nu} Re tr (R^{1x2}_{mu nu}(x) + R^{2x1}_{mu nu}(x))."""
+    return 0.5 * loop_trace(L, U, 1)
+
+
+def action_loops(L, U, c_plaq, c_rect):
+    _chk(U, np.complex128)
+    return lib().or_action_loops(_ptr(_L(L)), _ptr(U), float(c_plaq), float(c_rect))
+
+
+def force_loops(L, U, c_plaq, c_rect):
+    _chk(U, np.complex128)
+    F = new_mom(L)
+    lib().or_force_loops(_ptr(_L(L)), _ptr(U), float(c_plaq), float(c_rect), _ptr(F))
+    return F
+
+
+def loop_staple_count(kind, mu):
+    return lib().or_loop_staple_count(int(kind), int(mu))
+
+
+def md_trajectory(L, U, P, beta, tau, steps, integrator="QPQ", rho=(), lam=0.1931833275037836, c_rect=0.0):
+    """In place on U, P. Returns (H0, H1, dH). integrator: QPQ, PQP or OMELYAN.
+    c_rect: coefficient of the rectangle loops (thin links only)."""
     _chk(U, np.complex128)
     _chk(P, np.float64)
     out = np.zeros(3)
     r = _rho(rho)
     integ = {"QPQ": 0, "PQP": 1, "OMELYAN": 2}[integrator]
     lib().or_set_omelyan_lambda(float(lam))
-    lib().or_md_trajectory(_ptr(_L(L)), _ptr(U), _ptr(P), float(beta), float(tau), int(steps), integ, len(rho),
-                           _ptr(r), _ptr(out))
+    lib().or_set_rect(float(c_rect))
+    try:
+        lib().or_md_trajectory(_ptr(_L(L)), _ptr(U), _ptr(P), float(beta), float(tau), int(steps), integ, len(rho),
+                               _ptr(r), _ptr(out))
+    finally:
+        lib().or_set_rect(0.0)
     return tuple(out)
 
 

@@ -54,9 +54,12 @@ def _fake_library(oracle, log):
         if name == "gf_md_mom_update":
             _, P, U, eps, prm = args
             p = prm._obj
-            F = oracle.stout_force(list(P.L), U.U, rho_of(p), p.beta)
+            if p.c_rect != 0.0:
+                F = oracle.force_loops(list(P.L), U.U, 0.5 * p.beta, p.c_rect)
+            else:
+                F = oracle.stout_force(list(P.L), U.U, rho_of(p), p.beta)
             P.P += eps.value * F
-            log.append(("P", eps.value, p.beta))
+            log.append(("P", eps.value, p.beta, p.c_rect))
         elif name == "gf_md_link_update":
             _, U, P, eps, prm = args
             oracle.link_update(list(U.L), U.U, P.P, eps.value)
@@ -68,7 +71,7 @@ def _fake_library(oracle, log):
         elif name == "gf_hamiltonian":
             _, U, P, prm, out = args
             p = prm._obj
-            out._obj.value = oracle.hamiltonian(list(U.L), U.U, P.P, p.beta, rho_of(p))
+            out._obj.value = oracle.hamiltonian(list(U.L), U.U, P.P, p.beta, rho_of(p), c_rect=p.c_rect)
         else:
             raise AssertionError("the fake library has no %s" % name)
 

@@ -1,0 +1,211 @@
+"""Rectangle loops in the gauge action (push!(action, c, rect U rect'),
+make_loops_fromname("rectangular"); src/action/GaugeActions.jl,
+src/autostaples/wilsonloops.jl:304-330), e.g. the Iwasaki action
+beta (c0 plaq + c1 rect) with c1 = -0.331, c0 = 1 - 8 c1.
+
+The oracle builds the staples of any loop set by the rule of Wilsonloop's
+make_staple (each forward occurrence of U_mu contributes the rest of its
+loop); the CPU tests pin that rule on the plaquettes against the oracle's own
+Wilson force, and the rectangle force against finite differences of the
+rectangle potential. The GPU tests compare the fused fp64 kernels of
+gf_rect.cu with the oracle."""
+import numpy as np
+import pytest
+from scipy.linalg import expm
+
+from test_md_timescales import BETA, L4, _HostLinks, _HostMomenta, _fake_library, _split_actions  # noqa: F401
+from test_oracle import LAM
+
+C1 = -0.331
+C0 = 1 - 8 * C1
+B_IWA = 2.3
+CP, CR = 0.5 * B_IWA * C0, 0.5 * B_IWA * C1      # push! coefficients of plaq U plaq' and rect U rect'
+L6 = (6, 4, 4, 6)                                 # 576 sites: a partial last block of 128
+
+
+def _bump(oracle, U, mu, x, a, h):
+    M = oracle.mats(U.copy())
+    M[mu, x] = expm(1j * h * LAM[a] / 2) @ M[mu, x]
+    return oracle.from_mats(M)
+
+
+def test_loop_sets_and_staple_counts(oracle):
+    assert [oracle.loop_staple_count(0, mu) for mu in range(4)] == [6] * 4
+    assert [oracle.loop_staple_count(1, mu) for mu in range(4)] == [18] * 4
+    U = oracle.hot_start(list(L4), 3)
+    # the general rule on the plaquette set is the Wilson action and force
+    assert np.abs(oracle.force_loops(list(L4), U, 2.85, 0.0) - oracle.force(list(L4), U, 5.7)).max() < 1e-14
+    assert oracle.action_loops(list(L4), U, 2.85, 0.0) == pytest.approx(oracle.action(list(L4), U, 5.7), rel=1e-14)
+    assert 0.5 * oracle.loop_trace(list(L4), U, 0) == pytest.approx(oracle.plaquette(list(L4), U), rel=1e-14)
+    C = oracle.cold_start(list(L4))
+    assert oracle.rectangle_sum(list(L4), C) == 36 * 256
+    assert oracle.action_loops(list(L4), C, CP, CR) == pytest.approx(-(2 / 3) * (CP * 18 + CR * 36) * 256, rel=1e-15)
+
+
+@pytest.mark.parametrize("coefs", [(CP, CR), (0.0, 1.7)])
+def test_rectangle_force_is_minus_gradient_of_potential(oracle, coefs):
+    U = oracle.hot_start(list(L4), 7)
+    F = oracle.force_loops(list(L4), U, *coefs)
+    rng = np.random.RandomState(5)
+    h = 1e-4
+    for _ in range(6):
+        mu, x, a = rng.randint(4), rng.randint(256), rng.randint(8)
+        vp = oracle.action_loops(list(L4), _bump(oracle, U, mu, x, a, h), *coefs)
+        vm = oracle.action_loops(list(L4), _bump(oracle, U, mu, x, a, -h), *coefs)
+        assert (vp - vm) / (2 * h) == pytest.approx(-F[mu, x, a], rel=1e-6, abs=1e-7)
+
+
+def test_rectangle_sum_is_gauge_invariant(oracle):
+    from test_oracle import oracle_shift
+    U = oracle.hot_start(list(L4), 21)
+    G = oracle.mats(oracle.hot_start(list(L4), 22))[0]
+    M = oracle.mats(U)
+    Mt = np.empty_like(M)
+    for mu in range(4):
+        nb = np.array([oracle_shift(list(L4), x, mu) for x in range(256)])
+        Mt[mu] = G @ M[mu] @ np.conj(np.swapaxes(G[nb], -1, -2))
+    assert oracle.rectangle_sum(list(L4), oracle.from_mats(Mt)) == pytest.approx(oracle.rectangle_sum(list(L4), U),
+                                                                                 rel=1e-13)
+
+
+@pytest.mark.parametrize("integrator", ["QPQ", "PQP"])
+def test_iwasaki_md_is_reversible_and_second_order(oracle, integrator):
+    U0, P0 = oracle.hot_start(list(L4), 1234), oracle.gauss_mom(list(L4), 99)
+    U, P = U0.copy(), P0.copy()
+    oracle.md_trajectory(list(L4), U, P, B_IWA * C0, 0.5, 10, integrator, c_rect=CR)
+    oracle.md_trajectory(list(L4), U, P, B_IWA * C0, -0.5, 10, integrator, c_rect=CR)
+    assert np.abs(U - U0).max() < 2e-12 and np.abs(P - P0).max() < 2e-12
+    dh = []
+    for n in (10, 20):
+        U, P = U0.copy(), P0.copy()
+        dh.append(oracle.md_trajectory(list(L4), U, P, B_IWA * C0, 0.5, n, integrator, c_rect=CR)[2])
+    assert dh[0] / dh[1] == pytest.approx(4.0, rel=0.15)
+
+
+def test_action_api_with_rectangles(pkg):
+    a = pkg.GaugeAction(None)
+    pkg.push_(a, CP, ("plaquette", "plaquette_dag"))
+    pkg.push_(a, CR, "rectangular")
+    assert a.beta == pytest.approx(2 * CP) and a.c_rect == pytest.approx(CR)
+    with pytest.raises(ValueError):
+        pkg.push_(a, 1.0, "chair")
+    U = [None] * 4
+    drv = pkg.md_driver(U, a, steps=4)
+    p = drv.params()
+    assert p.beta == pytest.approx(2 * CP) and p.c_rect == pytest.approx(CR)
+    with pytest.raises(ValueError):
+        pkg.md_driver(U, a, steps=4, precision="mixed")
+    net = pkg.CovNeuralnet()
+    pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
+    with pytest.raises(ValueError):
+        pkg.md_driver(U, a, steps=4, smearing=net)
+
+
+def test_sexton_weingarten_with_a_rectangle_member(md, oracle):
+    """Plaquette member on the fast scale, rectangle member on the slow one:
+    the group kicks carry their own coefficients; reversible to 3e-12."""
+    p, log = md
+    api = p.api
+    fast, slow = api.GaugeAction(None), api.GaugeAction(None)
+    api.push_(fast, CP, "plaquette")
+    api.push_(slow, CR, "rectangular")
+    actions = api.MDActionSet(fast=fast, slow=slow)
+    sw = api.SextonWeingarten(slow="slow", fast="fast", n_fast=2)
+    Uh, Ph = oracle.hot_start(list(L4), 5), oracle.gauss_mom(list(L4), 6)
+    U0, P0 = Uh.copy(), Ph.copy()
+    U, P = _HostLinks(L4, Uh), _HostMomenta(L4, Ph)
+    api.md_trajectory_(U, P, api.md_driver(U, actions, steps=2, trajectory_length=0.2, integrator=sw),
+                       diagnostics=False)
+    kicks = {(e[2], e[3]) for e in log if e[0] == "P"}
+    assert kicks == {(2.0 * CP, 0.0), (0.0, CR)}
+    api.md_trajectory_(U, P, api.md_driver(U, actions, steps=2, trajectory_length=-0.2, integrator=sw),
+                       diagnostics=False)
+    assert np.abs(U.U - U0).max() < 3e-12 and np.abs(P.P - P0).max() < 3e-12
+
+
+@pytest.fixture
+def md(monkeypatch, oracle):
+    import __graft_entry__ as entry
+    from types import SimpleNamespace
+    pkg = entry.load_package()
+    import gaugefields_gb300.api as api
+    log = []
+    monkeypatch.setattr(api, "call", _fake_library(oracle, log))
+    return SimpleNamespace(pkg=pkg, api=api), log
+
+
+# ---------------------------------------------------------------------------
+# device
+# ---------------------------------------------------------------------------
+@pytest.mark.gpu
+@pytest.mark.parametrize("L", [(8, 8, 8, 8), L6])
+def test_rectangle_sum_action_and_force_match_the_oracle(pkg, oracle, L):
+    U = pkg.gauge_configuration(L, start="hot", seed=31)
+    Uh = U.to_host()
+    ref = oracle.rectangle_sum(list(L), Uh)
+    assert abs(pkg.rectangle_sum(U) - ref) <= 1e-13 * abs(ref)
+    a = pkg.GaugeAction(U)
+    pkg.push_(a, CP, "plaquette")
+    pkg.push_(a, CR, "rectangular")
+    v = pkg.md_potential(a, U)
+    vr = oracle.action_loops(list(L), Uh, CP, CR)
+    assert abs(v - vr) <= 1e-13 * abs(vr)
+    e = pkg.evaluate_GaugeAction(a, U)
+    assert abs(e + 3 * vr) <= 1e-13 * abs(vr)
+    F = pkg.gauge_momenta(U)
+    pkg.md_force_(F, a, U)
+    dF = np.abs(F.to_host() - oracle.force_loops(list(L), Uh, CP, CR)).max()
+    print("rectangle %s: sum rel %.2e  action rel %.2e  |dF| %.2e"
+          % (L, abs(pkg.rectangle_sum(U) - ref) / abs(ref), abs(v - vr) / abs(vr), dF))
+    assert dF < 1e-12
+    # cold start: every rectangle has trace 3
+    C = pkg.gauge_configuration(L, start="cold")
+    assert pkg.rectangle_sum(C) == 36 * int(np.prod(L))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("integrator", ["QPQ", "PQP"])
+def test_iwasaki_trajectory_matches_the_oracle(pkg, oracle, integrator):
+    """8^4 Haar start, Iwasaki beta = 2.3, tau = 0.5, 10 steps: Delta H to
+    1e-10, links and momenta to 1e-11 against the oracle with a
+    full-double-precision exponential."""
+    U = pkg.gauge_configuration((8, 8, 8, 8), start="hot", seed=41)
+    P = pkg.gaussian_momenta(U, seed=42)
+    Uh, Ph = U.to_host(), P.to_host()
+    a = pkg.GaugeAction(U)
+    pkg.push_(a, CP, "plaquette")
+    pkg.push_(a, CR, "rectangular")
+    integ = pkg.QPQ() if integrator == "QPQ" else pkg.PQP()
+    drv = pkg.md_driver(U, a, steps=10, trajectory_length=0.5, integrator=integ, reunitarize=False)
+    res = pkg.md_trajectory_(U, P, drv)
+    oracle.set_exp_method("taylor")
+    try:
+        h = oracle.md_trajectory([8, 8, 8, 8], Uh, Ph, 2 * CP, 0.5, 10, integrator, c_rect=CR)
+    finally:
+        oracle.set_exp_method("eigen")
+    du, dp = np.abs(U.to_host() - Uh).max(), np.abs(P.to_host() - Ph).max()
+    print("iwasaki %s: dH %.6e oracle %.6e  |dU| %.2e |dP| %.2e" % (integrator, res.delta_hamiltonian, h[2], du, dp))
+    assert abs(res.initial_hamiltonian - h[0]) <= 1e-13 * abs(h[0])
+    assert abs(res.delta_hamiltonian - h[2]) <= 1e-10
+    assert du < 1e-11 and dp < 1e-11
+
+
+@pytest.mark.gpu
+def test_rectangle_term_is_refused_outside_the_plain_form(pkg):
+    from gaugefields_gb300 import _lib
+    import ctypes
+    U = pkg.gauge_configuration(L4, start="hot", seed=1)
+    P = pkg.gauge_momenta(U)
+    a = pkg.GaugeAction(U)
+    pkg.push_(a, CP, "plaquette")
+    pkg.push_(a, CR, "rectangular")
+    p = pkg.md_driver(U, a, steps=2).params()
+    p.precision = _lib.GF_MIXED
+    with pytest.raises(Exception):
+        _lib.call("gf_md_mom_update", U.ctx.h, P.field.h, U.field.h, ctypes.c_double(0.1), ctypes.byref(p),
+                  ctx=U.ctx.h)
+    p.precision = _lib.GF_FP64
+    p.nstout, p.rho[0] = 1, 0.1
+    with pytest.raises(Exception):
+        _lib.call("gf_md_mom_update", U.ctx.h, P.field.h, U.field.h, ctypes.c_double(0.1), ctypes.byref(p),
+                  ctx=U.ctx.h)
