@@ -99,6 +99,7 @@ SIGNATURES = {
     "gf_stout_backward": [_P, _P, _P, _P],
     "gf_stout_mom_update": [_P, _P, _P, _P, _D, _D],
     "gf_flow": [_P, _P, _D, _I],
+    "gf_flow_loops": [_P, _P, _D, _I, _D, _D],
     "gf_flow_force": [_P, _P, _P, _D],
     "gf_prof_enable": [_P, _I],
     "gf_prof_read": [_P, _I, _DP, ctypes.POINTER(ctypes.c_longlong)],

@@ -28,7 +28,7 @@ __all__ = [
     "hmc_update_", "STOUT_Layer", "CovNeuralnet", "stout_smearing", "smear", "calc_smearedU", "back_prop",
     "Gradientflow", "gradient_flow", "flow_", "add_force_", "energy_density_plaquette", "substitute_U_",
     "similar", "clear_U_", "save_configuration", "load_configuration_", "Oneinstanton_SUN_embedded",
-    "MDActionSet", "MDForceGroup", "SextonWeingarten", "rectangle_sum",
+    "MDActionSet", "MDForceGroup", "SextonWeingarten", "rectangle_sum", "Gradientflow_general",
 ]
 
 
@@ -879,17 +879,52 @@ class Gradientflow:
         self.eps = float(eps)
 
 
-def gradient_flow(U, steps=1, step_size=0.01):
-    """gradient_flow(U; steps, step_size) (src/API.jl:420-437)."""
+class Gradientflow_general:
+    """Gradient flow of a general loop action (gradientflow.jl:42-118,
+    240-336): Gradientflow_general(U, linknames, linkvalues; Nflow, eps) with
+    the loop names "plaquette" and "rectangular" and real coefficients (each
+    set with its conjugate loops); the force is TA(U dS/dU)."""
+
+    def __init__(self, U, linknames, linkvalues, Nflow=1, eps=0.01):
+        names = [linknames] if isinstance(linknames, str) else list(linknames)
+        values = [linkvalues] if np.isscalar(linkvalues) else list(linkvalues)
+        if len(names) != len(values):
+            raise ValueError("one coefficient per loop name is needed; got %d names and %d values"
+                             % (len(names), len(values)))
+        self.c_plaq, self.c_rect = 0.0, 0.0
+        for n, v in zip(names, values):
+            if isinstance(v, complex) or not np.isreal(v):
+                raise ValueError("the GB300 backend takes real loop coefficients; got %r" % (v,))
+            if n == "plaquette":
+                self.c_plaq += float(v)
+            elif n == "rectangular":
+                self.c_rect += float(v)
+            else:
+                raise ValueError("the GB300 backend supports the plaquette and rectangular loops; got %r" % (n,))
+        self.Nflow = int(Nflow)
+        self.eps = float(eps)
+
+
+def gradient_flow(U, loops=None, coefficients=None, steps=1, step_size=0.01):
+    """gradient_flow(U; steps, step_size) and gradient_flow(U, loops,
+    coefficients; steps, step_size) (src/API.jl:420-438)."""
     if steps <= 0:
         raise ValueError("steps must be positive; got %d" % steps)
     if step_size <= 0:
         raise ValueError("step_size must be positive; got %s" % step_size)
-    return Gradientflow(U, Nflow=steps, eps=step_size)
+    if loops is None and coefficients is None:
+        return Gradientflow(U, Nflow=steps, eps=step_size)
+    if loops is None or coefficients is None:
+        raise ValueError("a general-action flow needs both loops and coefficients")
+    return Gradientflow_general(U, loops, coefficients, Nflow=steps, eps=step_size)
 
 
 def flow_(U, g):
-    """flow!(U, g) (gradientflow.jl:171-238)."""
+    """flow!(U, g) (gradientflow.jl:171-238; Gradientflow_general :240-336)."""
+    if isinstance(g, Gradientflow_general):
+        call("gf_flow_loops", U.ctx.h, U.field.h, ctypes.c_double(g.eps), int(g.Nflow), ctypes.c_double(g.c_plaq),
+             ctypes.c_double(g.c_rect), ctx=U.ctx.h)
+        return U
     call("gf_flow", U.ctx.h, U.field.h, ctypes.c_double(g.eps), int(g.Nflow), ctx=U.ctx.h)
     return U
 

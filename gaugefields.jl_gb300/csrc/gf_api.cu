@@ -831,6 +831,36 @@ extern "C" int gf_flow(gf_ctx* ctx, gf_field* U, double eps, int nsteps) {
   API_END(ctx)
 }
 
+// The same RK3 steps with the force TA(U dS/dU) of the plaquette + rectangle
+// action (Gradientflow_general); (c_plaq, c_rect) = (1, 0) is the Wilson flow.
+extern "C" int gf_flow_loops(gf_ctx* ctx, gf_field* U, double eps, int nsteps, double c_plaq, double c_rect) {
+  API_BEGIN
+  need(ctx && U, "gf_flow_loops: null argument");
+  need_ctx(ctx, U);
+  need_kind(U, GF_LINK64, "gf_flow_loops: U");
+  need(std::isfinite(eps) && eps != 0.0, "gf_flow_loops: eps must be finite and nonzero");
+  need(nsteps >= 0, "gf_flow_loops: nsteps must be nonnegative");
+  need(std::isfinite(c_plaq) && std::isfinite(c_rect), "gf_flow_loops: the coefficients must be finite");
+  if (!ctx->w_link64) ctx->w_link64 = field_new(ctx, GF_LINK64);
+  if (!ctx->w_link64b) ctx->w_link64b = field_new(ctx, GF_LINK64);
+  if (!ctx->w_mom[0]) ctx->w_mom[0] = field_new(ctx, GF_MOM64);
+  gf_field* W1 = ctx->w_link64;
+  gf_field* W2 = ctx->w_link64b;
+  gf_field* G = ctx->w_mom[0];
+  const double c0 = 17.0 * eps / 36.0;
+  const double c1 = -8.0 * eps / 9.0;
+  const double c2 = -0.75 * eps;
+  for (int n = 0; n < nsteps; ++n) {
+    loops_force_coef(ctx, U, G, c0 * c_plaq, c0 * c_rect, 0.0);    // G = 17eps/36 F0
+    exp_mom_links(ctx, W1, G, -9.0 / 17.0, U);                    // W1 = exp(-eps/4 F0) U
+    loops_force_coef(ctx, W1, G, c1 * c_plaq, c1 * c_rect, 1.0);   // G += -8eps/9 F1
+    exp_mom_links(ctx, W2, G, 1.0, W1);                           // W2 = exp(G) W1
+    loops_force_coef(ctx, W2, G, c2 * c_plaq, c2 * c_rect, -1.0);  // G = -G - 3eps/4 F2
+    exp_mom_links(ctx, U, G, 1.0, W2);                            // U = exp(G) W2
+  }
+  API_END(ctx)
+}
+
 // ---------------------------------------------------------------------------
 // instrumentation
 // ---------------------------------------------------------------------------

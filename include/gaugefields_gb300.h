@@ -224,6 +224,12 @@ int gf_stout_mom_update(gf_ctx* ctx, gf_stout* st, gf_field* P, const gf_field* 
 /* flow!(U, ::Gradientflow) (smearing/gradientflow.jl:171-238): nsteps RK3
  * Wilson-flow steps of size eps. */
 int gf_flow(gf_ctx* ctx, gf_field* U, double eps, int nsteps);
+/* flow!(U, ::Gradientflow_general) (smearing/gradientflow.jl:240-336) for the
+ * action with the plaquette loops at c_plaq and the rectangle loops at c_rect
+ * (gradient_flow(U, [:plaquette, :rectangular], [c_plaq, c_rect]), API.jl:
+ * 426-438): the same RK3 steps with the force TA(U dS/dU) (F_update!,
+ * gradientflow.jl:319-334), fp64. (1, 0) is the Wilson flow of gf_flow. */
+int gf_flow_loops(gf_ctx* ctx, gf_field* U, double eps, int nsteps, double c_plaq, double c_rect);
 /* add_force!(F, U, temps; plaqonly=true) (AbstractGaugefields.jl:2717-2763):
  * F += factor * TA(U_mu V_mu^dag) with V the six-staple sum. */
 int gf_flow_force(gf_ctx* ctx, const gf_field* U, gf_field* F, double factor);

@@ -759,10 +759,11 @@ double or_action_loops(const int L[4], const cdbl* U, double c_plaq, double c_re
   return -v / 3.0;
 }
 
-/* md_force! of the same action: F_mu = TA-coefficients of -(1/3) U_mu dS/dU_mu,
- * dS/dU_mu = sum over the sets of c * (staples of U_mu) (calc_dSdUμ!,
- * src/action/GaugeActions.jl:95-123) */
-void or_force_loops(const int L[4], const cdbl* U, double c_plaq, double c_rect, double* F) {
+/* F_mu (+)= factor * TA-coefficients of U_mu dS/dU_mu with dS/dU_mu = sum over
+ * the sets of c * (staples of U_mu) (calc_dSdUμ!, src/action/GaugeActions.jl:
+ * 95-123); accumulate = 0 overwrites F. */
+static void loops_force(const int L[4], const cdbl* U, double c_plaq, double c_rect, double factor, int accumulate,
+                        double* F) {
   Lat lat = mklat(L);
   Loop lp[12], lr[24];
   int np = loop_set(0, lp), nr = loop_set(1, lr);
@@ -785,10 +786,16 @@ void or_force_loops(const int L[4], const cdbl* U, double c_plaq, double c_rect,
       M3 u = ld(U, &lat, mu, x);
       M3 w = mmul(&u, &acc);
       double* f = F + ((size_t)mu * lat.V + x) * 8;
-      for (int a = 0; a < 8; ++a) f[a] = 0;
-      ta_add(f, -1.0 / 3.0, &w);
+      if (!accumulate)
+        for (int a = 0; a < 8; ++a) f[a] = 0;
+      ta_add(f, factor, &w);
     }
   }
+}
+
+/* md_force! of the same action: F_mu = TA-coefficients of -(1/3) U_mu dS/dU_mu */
+void or_force_loops(const int L[4], const cdbl* U, double c_plaq, double c_rect, double* F) {
+  loops_force(L, U, c_plaq, c_rect, -1.0 / 3.0, 0, F);
 }
 
 /* number of staples of U_mu in a set (6 for the plaquettes, 18 for the
@@ -1187,6 +1194,42 @@ void or_flow(const int L[4], cdbl* U, double eps, int nsteps) {
     exp_af_u(&lat, W2, 1.0, Ft, W1);
     memset(F2, 0, sizeof(double) * nf);
     or_flow_force(L, W2, F2, 1.0);
+    memset(Ft, 0, sizeof(double) * nf);
+    mom_axpy(&lat, Ft, -(3 * eps / 4), F2);
+    mom_axpy(&lat, Ft, 8 * eps / 9, F1);
+    mom_axpy(&lat, Ft, -(17 * eps / 36), F0);
+    exp_af_u(&lat, U, 1.0, Ft, W2);
+  }
+  free(F0);
+  free(F1);
+  free(F2);
+  free(Ft);
+  free(W1);
+  free(W2);
+}
+
+/* flow!(U, ::Gradientflow_general) (src/smearing/gradientflow.jl:240-336): the
+ * same RK3 steps with the force F_update!(F, U, 1, Dim, action) = TA(U dS/dU)
+ * of the action holding c_plaq (plaq U plaq') and c_rect (rect U rect'),
+ * gradient_flow(U, loops, coefficients) of src/API.jl:426-438. */
+void or_flow_loops(const int L[4], cdbl* U, double eps, int nsteps, double c_plaq, double c_rect) {
+  Lat lat = mklat(L);
+  size_t nf = (size_t)32 * lat.V, nl = (size_t)36 * lat.V;
+  double* F0 = (double*)malloc(sizeof(double) * nf);
+  double* F1 = (double*)malloc(sizeof(double) * nf);
+  double* F2 = (double*)malloc(sizeof(double) * nf);
+  double* Ft = (double*)malloc(sizeof(double) * nf);
+  cdbl* W1 = (cdbl*)malloc(sizeof(cdbl) * nl);
+  cdbl* W2 = (cdbl*)malloc(sizeof(cdbl) * nl);
+  for (int s = 0; s < nsteps; ++s) {
+    loops_force(L, U, c_plaq, c_rect, 1.0, 0, F0);
+    exp_af_u(&lat, W1, -eps / 4, F0, U);
+    loops_force(L, W1, c_plaq, c_rect, 1.0, 0, F1);
+    memset(Ft, 0, sizeof(double) * nf);
+    mom_axpy(&lat, Ft, -(8 * eps / 9), F1);
+    mom_axpy(&lat, Ft, 17 * eps / 36, F0);
+    exp_af_u(&lat, W2, 1.0, Ft, W1);
+    loops_force(L, W2, c_plaq, c_rect, 1.0, 0, F2);
     memset(Ft, 0, sizeof(double) * nf);
     mom_axpy(&lat, Ft, -(3 * eps / 4), F2);
     mom_axpy(&lat, Ft, 8 * eps / 9, F1);

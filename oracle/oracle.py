@@ -82,6 +82,7 @@ def _declare(l):
         "or_force_loops": ([_P, _P, _D, _D, _P], None),
         "or_loop_staple_count": ([_I, _I], _I),
         "or_set_rect": ([_D], None),
+        "or_flow_loops": ([_P, _P, _D, _I, _D, _D], None),
     }
     for name, (args, res) in sig.items():
         f = getattr(l, name)
@@ -282,6 +283,12 @@ def force_loops(L, U, c_plaq, c_rect):
     F = new_mom(L)
     lib().or_force_loops(_ptr(_L(L)), _ptr(U), float(c_plaq), float(c_rect), _ptr(F))
     return F
+
+
+def flow_loops(L, U, eps, nsteps, c_plaq, c_rect):
+    """Gradientflow_general with the plaquette and rectangle loops, in place."""
+    _chk(U, np.complex128)
+    lib().or_flow_loops(_ptr(_L(L)), _ptr(U), float(eps), int(nsteps), float(c_plaq), float(c_rect))
 
 
 def loop_staple_count(kind, mu):

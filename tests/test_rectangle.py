@@ -209,3 +209,76 @@ def test_rectangle_term_is_refused_outside_the_plain_form(pkg):
     with pytest.raises(Exception):
         _lib.call("gf_md_mom_update", U.ctx.h, P.field.h, U.field.h, ctypes.c_double(0.1), ctypes.byref(p),
                   ctx=U.ctx.h)
+
+
+# ---------------------------------------------------------------------------
+# general flow (Gradientflow_general, src/smearing/gradientflow.jl:240-336)
+# ---------------------------------------------------------------------------
+def test_general_flow_with_plaquettes_is_the_wilson_flow(oracle):
+    """F_update! with the plaquette set at coefficient 1 is add_force!(plaqonly):
+    the two flows agree to rounding (exact exponential)."""
+    oracle.set_exp_method("taylor")
+    try:
+        U = oracle.uniform_hot_start(list(L4), 123)
+        V = U.copy()
+        oracle.flow(list(L4), U, 0.01, 10)
+        oracle.flow_loops(list(L4), V, 0.01, 10, 1.0, 0.0)
+    finally:
+        oracle.set_exp_method("eigen")
+    assert np.abs(U - V).max() < 1e-14
+
+
+def test_general_flow_lowers_the_iwasaki_action(oracle):
+    U = oracle.hot_start(list(L4), 5)
+    s = [oracle.action_loops(list(L4), U, C0, C1)]
+    for _ in range(4):
+        oracle.flow_loops(list(L4), U, 0.01, 5, C0, C1)
+        s.append(oracle.action_loops(list(L4), U, C0, C1))
+    assert all(b < a for a, b in zip(s, s[1:]))
+
+
+def test_general_flow_api(pkg, monkeypatch):
+    import gaugefields_gb300.api as api
+    g = pkg.gradient_flow(None, ["plaquette", "rectangular"], [C0, C1], steps=7, step_size=0.02)
+    assert isinstance(g, pkg.Gradientflow_general)
+    assert (g.c_plaq, g.c_rect, g.Nflow, g.eps) == (C0, C1, 7, 0.02)
+    assert isinstance(pkg.gradient_flow(None, steps=3), pkg.Gradientflow)
+    with pytest.raises(ValueError):
+        pkg.gradient_flow(None, ["plaquette"], None)
+    with pytest.raises(ValueError):
+        pkg.Gradientflow_general(None, ["plaquette", "rectangular"], [1.0])
+    with pytest.raises(ValueError):
+        pkg.Gradientflow_general(None, ["chair"], [1.0])
+    with pytest.raises(ValueError):
+        pkg.Gradientflow_general(None, ["plaquette"], [1.0 + 0.5j])
+    seen = []
+    monkeypatch.setattr(api, "call", lambda name, *args, ctx=None: seen.append((name, args)))
+    from types import SimpleNamespace
+    U = SimpleNamespace(ctx=SimpleNamespace(h="ctx"), field=SimpleNamespace(h="U"))
+    pkg.flow_(U, g)
+    name, args = seen[0]
+    assert name == "gf_flow_loops" and args[:2] == ("ctx", "U") and args[2].value == 0.02 and args[3] == 7
+    assert (args[4].value, args[5].value) == (C0, C1)
+
+
+@pytest.mark.gpu
+def test_general_flow_matches_the_oracle(pkg, oracle):
+    """4^4 Haar start, Iwasaki loops (c0, c1), 10 steps of 0.01: links to
+    1e-12 against the oracle with the exact exponential; the (1, 0) flow is
+    the Wilson flow of gf_flow to 1e-12."""
+    U = pkg.gauge_configuration(L4, start="hot", seed=9)
+    Uh = U.to_host()
+    pkg.flow_(U, pkg.gradient_flow(U, ["plaquette", "rectangular"], [C0, C1], steps=10, step_size=0.01))
+    oracle.set_exp_method("taylor")
+    try:
+        oracle.flow_loops(list(L4), Uh, 0.01, 10, C0, C1)
+    finally:
+        oracle.set_exp_method("eigen")
+    d = np.abs(U.to_host() - Uh).max()
+    A = pkg.gauge_configuration(L4, start="hot", seed=9)
+    B = pkg.gauge_configuration(L4, start="hot", seed=9)
+    pkg.flow_(A, pkg.Gradientflow(A, Nflow=10, eps=0.01))
+    pkg.flow_(B, pkg.Gradientflow_general(B, "plaquette", 1.0, Nflow=10, eps=0.01))
+    dw = np.abs(A.to_host() - B.to_host()).max()
+    print("general flow: |dU| vs oracle %.2e, vs Wilson flow %.2e" % (d, dw))
+    assert d < 1e-12 and dw < 1e-12
