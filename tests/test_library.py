@@ -61,6 +61,12 @@ def test_null_arguments_are_rejected(pkg):
     assert lib.gf_md_mom_update(None, None, None, ctypes.c_double(0.1), ctypes.byref(prm)) == _lib.GF_EINVAL
     assert lib.gf_md_link_update(None, None, None, ctypes.c_double(0.1), ctypes.byref(prm)) == _lib.GF_EINVAL
     assert lib.gf_stout_create(None, 2, None, _lib.GF_DFLOAT, 1, None) == _lib.GF_EINVAL
+    assert lib.gf_rectangle(None, None, ctypes.byref(out)) == _lib.GF_EINVAL
+    assert lib.gf_action_loops(None, None, ctypes.c_double(1.0), ctypes.c_double(0.1), ctypes.byref(out)) == \
+        _lib.GF_EINVAL
+    assert lib.gf_force_loops(None, None, ctypes.c_double(1.0), ctypes.c_double(0.1), None) == _lib.GF_EINVAL
+    assert lib.gf_flow_loops(None, None, ctypes.c_double(0.01), 1, ctypes.c_double(1.0), ctypes.c_double(0.1)) == \
+        _lib.GF_EINVAL
     assert lib.gf_field_free(None) == _lib.GF_OK
     assert lib.gf_ctx_destroy(None) == _lib.GF_OK
 
@@ -88,8 +94,10 @@ def test_md_driver_argument_validation(pkg):
         pkg.md_driver(U, action, steps=10, trajectory_length=0.0)
     with pytest.raises(ValueError):
         pkg.md_driver(U, action, steps=10, trajectory_length=float("inf"))
-    with pytest.raises(ValueError):
-        pkg.md_driver(U, action, steps=10, integrator=object())
+    # an integrator without md_step! fails when it steps (test/md_driver.jl:309-320)
+    odd = pkg.md_driver(U, action, steps=10, integrator=object())
+    with pytest.raises(ValueError, match="md_step! is not implemented"):
+        pkg.md_trajectory_(U, None, odd, diagnostics=False)
     with pytest.raises(ValueError):
         pkg.md_driver(U, pkg.GaugeAction(U), steps=10)  # empty action
     drv = pkg.md_driver(U, action, steps=10, trajectory_length=-1.0, integrator=pkg.PQP())
