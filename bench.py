@@ -67,6 +67,8 @@ def algorithmic_bytes_per_link(kclass):
         # one link read per link (four directions per site)
         "plaquette": 144,
         "force": link + 128,
+        # plaquette + rectangle force (fp64 links): U in, P read + write
+        "rect": 144 + 128,
     }.get(base)
 
 
@@ -85,6 +87,9 @@ def algorithmic_flops_per_link(kclass):
         "link_update": 2 * mm + 400,
         "plaquette": 2 * mm * 6 / 4.0,
         "force": staples + mm,
+        # per axis 2 plaquette staples (mul + mac) and 6 rectangle staples
+        # (3 mul + 1 mac each), then U (c_p S + c_r R)
+        "rect": 3 * (2 * mm + 2 * mac + 18 * mm + 6 * mac) + mm,
     }.get(base)
 
 
