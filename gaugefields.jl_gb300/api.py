@@ -443,10 +443,11 @@ class OmelyanPQP:
 class MDActionSet:
     """MDActionSet(; name=action, ...) (molecular_dynamics.jl:45-66): named
     action providers whose potentials and forces add. On this backend the
-    members are Wilson plaquette actions on the driver's (possibly smeared)
-    links. Their forces are linear in the couplings, so the force of any
-    group of members is the force of one Wilson action with the group's
-    summed beta: a group's momentum update is one fused force pass."""
+    members are GaugeActions of plaquette (and, in the plain fp64 form on thin
+    links, rectangle) loops on the driver's links. Their forces are linear in
+    the loop coefficients, so the force of any group of members is the force
+    of one action with the group's summed coefficients: a group's momentum
+    update is one fused force pass."""
 
     def __init__(self, terms=None, **named):
         terms = dict(terms or {}, **named)
