@@ -47,3 +47,15 @@ def test_single_process_needs_no_collective():
     import torch
     import bench
     assert bench.max_over_ranks(torch, None, 2.0, "cpu") == 2.0
+
+
+def test_every_kernel_class_has_roofline_figures(pkg):
+    """bench.py's algorithmic bytes and flops cover every kernel class the
+    library times, except the catch-all class of starts and copies."""
+    import bench
+    from gaugefields_gb300 import _lib
+    for k in _lib.KERNEL_CLASSES:
+        if k == "other":
+            continue
+        assert bench.algorithmic_bytes_per_link(k) > 0 and bench.algorithmic_flops_per_link(k) > 0, k
+        assert k in _lib.KERNEL_PRECISION, k
