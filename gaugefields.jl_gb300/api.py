@@ -773,11 +773,27 @@ HMCResult = namedtuple("HMCResult", ["initial_hamiltonian", "final_hamiltonian",
 
 
 def hmc_update_(U, P, driver, seed, sweep, unif):
-    """Momentum refresh + md_trajectory! + Metropolis (docs/src/hmc.md:22-81);
-    a rejected trajectory restores U."""
+    """Momentum refresh + md_trajectory! + Metropolis (docs/src/hmc.md:22-81):
+    accept when Delta H <= 0 or unif < exp(-Delta H); a rejected trajectory
+    restores U, and a non-finite Delta H restores U and raises. The builtin
+    integrators run as one native call (gf_hmc_update); SextonWeingarten and
+    custom integrators take the same steps from the host (a device copy of
+    the links, gaussian_momenta_, md_trajectory_, the same test)."""
+    if not 0.0 <= unif < 1.0:
+        raise ValueError("unif must be in [0,1); got %s" % (unif,))
     if not isinstance(driver.integrator, (QPQ, PQP, OmelyanPQP)):
-        raise ValueError("hmc_update_ runs the builtin integrators natively; for %s use gaussian_momenta_, "
-                         "md_trajectory_ and the Metropolis test on the host" % type(driver.integrator).__name__)
+        backup = U.similar()
+        substitute_U_(backup, U)
+        gaussian_momenta_(P, seed=seed, sweep=sweep)
+        res = md_trajectory_(U, P, driver)
+        dh = res.delta_hamiltonian
+        finite = math.isfinite(dh)
+        accept = finite and (dh <= 0.0 or unif < math.exp(-dh))
+        if not accept:
+            substitute_U_(U, backup)
+        if not finite:
+            raise _lib.GFNonFinite(_lib.GF_ENAN, "hmc_update_: Delta H is not finite; configuration restored")
+        return HMCResult(res.initial_hamiltonian, res.final_hamiltonian, dh, accept)
     p = driver.params()
     out = (ctypes.c_double * 4)()
     call("gf_hmc_update", U.ctx.h, U.field.h, P.field.h, ctypes.byref(p), ctypes.c_uint64(int(seed)),

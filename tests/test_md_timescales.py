@@ -32,6 +32,9 @@ class _HostLinks:
     def __len__(self):
         return 4
 
+    def similar(self):
+        return _HostLinks(self.L, np.zeros_like(self.U))
+
 
 class _HostMomenta:
     def __init__(self, L, P):
@@ -68,6 +71,12 @@ def _fake_library(oracle, log):
             _, U, beta, F = args
             F.P[...] = oracle.force(list(U.L), U.U, beta.value)
             log.append(("F", beta.value))
+        elif name == "gf_field_copy":
+            _, dst, src = args
+            dst.U[...] = src.U
+        elif name == "gf_gaussian_momenta":
+            _, P, seed, sweep = args
+            P.P[...] = oracle.gauss_mom(list(P.L), seed.value, sweep.value)
         elif name == "gf_hamiltonian":
             _, U, P, prm, out = args
             p = prm._obj
@@ -250,3 +259,29 @@ def test_sexton_weingarten_on_the_device_matches_the_oracle(pkg, pkg_host, oracl
                                                            integrator=sw))
         assert np.abs(Ud - Uo.U).max() < 1e-10 and np.abs(Pd - Po.P).max() < 1e-10
         assert abs(dev.delta_hamiltonian - ref.delta_hamiltonian) < 1e-10
+
+
+def test_hmc_update_with_sexton_weingarten(md, oracle):
+    """hmc_update_ for a non-builtin integrator: momentum refresh from (seed,
+    sweep), the trajectory, Metropolis (accept when dH <= 0 or unif <
+    exp(-dH)); a rejection restores the links exactly."""
+    p, _ = md
+    api = p.api
+    actions = _split_actions(api, {"slow": 0.75 * BETA, "fast": 0.25 * BETA})
+    sw = api.SextonWeingarten(slow="slow", fast="fast", n_fast=2)
+    U0 = oracle.hot_start(list(L4), 8)
+    U, P = _HostLinks(L4, U0.copy()), _HostMomenta(L4, np.zeros((4, 256, 8)))
+    drv = api.md_driver(U, actions, steps=3, trajectory_length=0.3, integrator=sw)
+    res = api.hmc_update_(U, P, drv, seed=17, sweep=2, unif=0.0)
+    assert res.accepted and np.abs(U.U - U0).max() > 1e-3
+    # the same trajectory composed by hand
+    V, Q = _HostLinks(L4, U0.copy()), _HostMomenta(L4, oracle.gauss_mom(list(L4), 17, 2))
+    ref = api.md_trajectory_(V, Q, drv)
+    assert res.delta_hamiltonian == ref.delta_hamiltonian and np.array_equal(U.U, V.U)
+    # a coarse trajectory (dH >> 1) is rejected at unif close to 1 and restores U
+    coarse = api.md_driver(U, actions, steps=1, trajectory_length=2.0, integrator=sw)
+    before = U.U.copy()
+    res = api.hmc_update_(U, P, coarse, seed=18, sweep=0, unif=1.0 - 1e-15)
+    assert res.delta_hamiltonian > 1.0 and not res.accepted and np.array_equal(U.U, before)
+    with pytest.raises(ValueError):
+        api.hmc_update_(U, P, coarse, seed=18, sweep=0, unif=1.0)
