@@ -77,6 +77,7 @@ SIGNATURES = {
     "gf_cold_start": [_P, _P],
     "gf_hot_start": [_P, _P, _U64],
     "gf_gaussian_momenta": [_P, _P, _U64, _U64],
+    "gf_mom_scale": [_P, _P, _D],
     "gf_reunitarize": [_P, _P],
     "gf_plaquette": [_P, _P, _DP],
     "gf_action": [_P, _P, _D, _DP],

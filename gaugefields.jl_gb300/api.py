@@ -341,16 +341,19 @@ def gauge_momenta(U):
 
 
 def gaussian_momenta_(momenta, sigma=1.0, seed=None, sweep=0):
-    """gaussian_momenta!(P; seed, sweep) (src/API.jl:341-368): p_a ~ N(0, sigma^2)."""
+    """gaussian_momenta!(P; seed, sweep, sigma) (src/API.jl:341-368): p_a ~
+    N(0, sigma^2), the unit-variance draws of (seed, sweep) scaled by sigma."""
     if sweep < 0:
         raise ValueError("sweep must be nonnegative; got %d" % sweep)
-    if sigma != 1.0:
-        raise ValueError("the device generator draws unit-variance momenta")
+    if not math.isfinite(sigma):
+        raise ValueError("sigma must be finite; got %s" % (sigma,))
     if seed is None:
         seed = int.from_bytes(os.urandom(8), "little")
     P = momenta
     call("gf_gaussian_momenta", P.ctx.h, P.field.h, ctypes.c_uint64(int(seed)), ctypes.c_uint64(int(sweep)),
          ctx=P.ctx.h)
+    if sigma != 1.0:
+        call("gf_mom_scale", P.ctx.h, P.field.h, ctypes.c_double(sigma), ctx=P.ctx.h)
     return P
 
 

@@ -303,6 +303,16 @@ extern "C" int gf_gaussian_momenta(gf_ctx* ctx, gf_field* P, uint64_t seed, uint
   gaussian_momenta(ctx, P, seed, sweep);
   API_END(ctx)
 }
+
+extern "C" int gf_mom_scale(gf_ctx* ctx, gf_field* P, double a) {
+  API_BEGIN
+  need(ctx && P, "gf_mom_scale: null argument");
+  need_ctx(ctx, P);
+  need_kind(P, GF_MOM64, "gf_mom_scale: P");
+  need(std::isfinite(a), "gf_mom_scale: the factor must be finite");
+  mom_scale(ctx, P, a);
+  API_END(ctx)
+}
 extern "C" int gf_reunitarize(gf_ctx* ctx, gf_field* U) {
   API_BEGIN
   need(ctx && U, "gf_reunitarize: null argument");

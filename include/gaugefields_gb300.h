@@ -136,6 +136,9 @@ int gf_cold_start(gf_ctx* ctx, gf_field* U);
 int gf_hot_start(gf_ctx* ctx, gf_field* U, uint64_t seed);
 /* gaussian_momenta!(P; seed, sweep) (API.jl:341-368): p_a ~ N(0,1). */
 int gf_gaussian_momenta(gf_ctx* ctx, gf_field* P, uint64_t seed, uint64_t sweep);
+/* P <- a P on a MOM64 field: gaussian_momenta!(P; sigma) (API.jl:341-368)
+ * draws unit-variance momenta and scales them by sigma. */
+int gf_mom_scale(gf_ctx* ctx, gf_field* P, double a);
 /* normalize_U! (AbstractGaugefields.jl:3378-3457) on every link. */
 int gf_reunitarize(gf_ctx* ctx, gf_field* U);
 

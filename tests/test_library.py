@@ -62,6 +62,7 @@ def test_null_arguments_are_rejected(pkg):
     assert lib.gf_md_link_update(None, None, None, ctypes.c_double(0.1), ctypes.byref(prm)) == _lib.GF_EINVAL
     assert lib.gf_stout_create(None, 2, None, _lib.GF_DFLOAT, 1, None) == _lib.GF_EINVAL
     assert lib.gf_rectangle(None, None, ctypes.byref(out)) == _lib.GF_EINVAL
+    assert lib.gf_mom_scale(None, None, ctypes.c_double(0.5)) == _lib.GF_EINVAL
     assert lib.gf_action_loops(None, None, ctypes.c_double(1.0), ctypes.c_double(0.1), ctypes.byref(out)) == \
         _lib.GF_EINVAL
     assert lib.gf_force_loops(None, None, ctypes.c_double(1.0), ctypes.c_double(0.1), None) == _lib.GF_EINVAL
@@ -195,3 +196,23 @@ def test_double_float_op_tables_stay_in_bounds():
     # the placeholders resolve to fields 1, 2 or slots 4, 5 (src 7, 8)
     assert "recompute ? 8 : 2" in src and "TOP ? 7 : 1" in src
     assert nslots["c_local_ops"] >= 6
+
+
+def test_gaussian_momenta_sigma_scales_the_unit_draws(pkg, monkeypatch):
+    """gaussian_momenta!(P; sigma): the unit-variance draws of (seed, sweep),
+    then P <- sigma P (gf_mom_scale); sigma = 1 makes no second call."""
+    import gaugefields_gb300.api as api
+    from types import SimpleNamespace
+    P = SimpleNamespace(ctx=SimpleNamespace(h="ctx"), field=SimpleNamespace(h="P"))
+    seen = []
+    monkeypatch.setattr(api, "call", lambda name, *args, ctx=None: seen.append((name, args)))
+    pkg.gaussian_momenta_(P, sigma=0.5, seed=7, sweep=3)
+    assert [n for n, _ in seen] == ["gf_gaussian_momenta", "gf_mom_scale"]
+    assert (seen[0][1][2].value, seen[0][1][3].value) == (7, 3) and seen[1][1][2].value == 0.5
+    seen.clear()
+    pkg.gaussian_momenta_(P, seed=7, sweep=3)
+    assert [n for n, _ in seen] == ["gf_gaussian_momenta"]
+    with pytest.raises(ValueError):
+        pkg.gaussian_momenta_(P, sigma=float("nan"), seed=7)
+    with pytest.raises(ValueError):
+        pkg.gaussian_momenta_(P, sweep=-1, seed=7)
