@@ -99,6 +99,8 @@ SIGNATURES = {
     "gf_stout_forward": [_P, _P, _P, _P],
     "gf_stout_backward": [_P, _P, _P, _P],
     "gf_stout_mom_update": [_P, _P, _P, _P, _D, _D],
+    "gf_stout_param_derivatives": [_P, _P, _P, _P, _P],
+    "gf_field_axpy": [_P, _P, _D, _P],
     "gf_flow": [_P, _P, _D, _I],
     "gf_flow_loops": [_P, _P, _D, _I, _D, _D],
     "gf_flow_force": [_P, _P, _P, _D],

@@ -26,8 +26,9 @@ __all__ = [
     "QPQ", "PQP", "OmelyanPQP", "md_driver", "md_step_size", "md_hamiltonian", "md_potential", "md_force_",
     "md_action_workspace", "update_gaugefields_", "update_momenta_", "md_step_", "md_trajectory_",
     "hmc_update_", "STOUT_Layer", "CovNeuralnet", "stout_smearing", "smear", "calc_smearedU", "back_prop",
+    "get_parameter_derivatives",
     "Gradientflow", "gradient_flow", "flow_", "add_force_", "energy_density_plaquette", "substitute_U_",
-    "similar", "clear_U_", "save_configuration", "load_configuration_", "Oneinstanton_SUN_embedded",
+    "similar", "clear_U_", "normalize_U_", "save_configuration", "load_configuration_", "Oneinstanton_SUN_embedded",
     "MDActionSet", "MDForceGroup", "SextonWeingarten", "rectangle_sum", "Gradientflow_general",
 ]
 
@@ -302,6 +303,15 @@ def substitute_U_(A, B):
 
 def clear_U_(A):
     call("gf_field_zero", A.ctx.h, A.field.h, ctx=A.ctx.h)
+
+
+def normalize_U_(U):
+    """normalize_U!(U) (src/AbstractGaugefields.jl:3378-3457, normalize3! per
+    link): Gram-Schmidt of rows 1-2, row 3 the conjugate cross product, in
+    fp64 on the device."""
+    if U.field.kind != _lib.GF_LINK64:
+        raise ValueError("normalize_U_ needs an fp64 link field")
+    call("gf_reunitarize", U.ctx.h, U.field.h, ctx=U.ctx.h)
 
 
 def calculate_Plaquette(U, temp=None, staple=None):
@@ -887,6 +897,24 @@ def back_prop(dSdUbar, smearing, history, U):
     out = Gaugefields4D(U.ctx, _lib.GF_MAT64)
     call("gf_stout_backward", U.ctx.h, history.h, dSdUbar.field.h, out.field.h, ctx=U.ctx.h)
     return out
+
+
+def get_parameter_derivatives(dSdUbar, smearing, U, precision="fp64"):
+    """get_parameter_derivatives(δL, net, Uout_multi, Uin) (Abstractsmearing.jl:
+    416-436, with parameter_derivatives of each STOUT_Layer, stout_fast.jl:
+    371-386): dS/drho of every layer of `smearing` on the thin links U, given
+    dS/dUbar of the top level (a general 3x3 fp64 field). Returns a list with
+    one value per layer."""
+    rhos = smearing.rhos()
+    stack = _StoutStack(U.ctx, rhos, precision)
+    if precision == "mixed":
+        d = Gaugefields4D(U.ctx, _lib.GF_MAT32)
+        call("gf_field_copy", U.ctx.h, d.field.h, dSdUbar.field.h, ctx=U.ctx.h)
+    else:
+        d = dSdUbar
+    out = (ctypes.c_double * len(rhos))()
+    call("gf_stout_param_derivatives", U.ctx.h, stack.h, U.field.h, d.field.h, out, ctx=U.ctx.h)
+    return list(out)
 
 
 # ---------------------------------------------------------------------------

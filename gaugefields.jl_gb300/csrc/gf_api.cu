@@ -91,11 +91,14 @@ extern "C" int gf_ctx_create(const int L[4], int device, gf_ctx** out) {
   for (int i = 0; i < 4; ++i) {
     need(L[i] >= 2 && (L[i] % 2) == 0, "gf_ctx_create: every lattice extent must be even and >= 2");
     V *= L[i];
+    // checked after every factor: the running product stays below 2^28 before
+    // the next multiply, so it cannot overflow
+    need(V <= (1LL << 28), "gf_ctx_create: volume too large for 32-bit site indices");
   }
-  need(V <= (1LL << 28), "gf_ctx_create: volume too large for 32-bit site indices");
   GF_CUDA(cudaSetDevice(device));
   ctx = new gf_ctx();
   ctx->device = device;
+  GF_CUDA(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device));
   for (int i = 0; i < 4; ++i) ctx->geom.L[i] = L[i];
   ctx->geom.vol = (int)V;
   ctx->geom.vh = (int)(V / 2);
@@ -247,6 +250,19 @@ extern "C" int gf_field_zero(gf_ctx* ctx, gf_field* f) {
   API_END(ctx)
 }
 
+extern "C" int gf_field_axpy(gf_ctx* ctx, gf_field* y, double a, const gf_field* x) {
+  API_BEGIN
+  need(ctx && y && x, "gf_field_axpy: null argument");
+  need_ctx(ctx, y);
+  need_ctx(ctx, x);
+  need(y->kind == x->kind, "gf_field_axpy: the fields must be of one kind");
+  need(y->kind == GF_LINK64 || y->kind == GF_MAT64 || y->kind == GF_MOM64,
+       "gf_field_axpy: fp64 fields (LINK64, MAT64, MOM64) only");
+  need(std::isfinite(a), "gf_field_axpy: the factor must be finite");
+  field_axpy(ctx, y, a, x);
+  API_END(ctx)
+}
+
 // ---------------------------------------------------------------------------
 // host transfer
 // ---------------------------------------------------------------------------
@@ -390,8 +406,10 @@ static gf_stout* stout_new(gf_ctx* ctx, int nlev, const double* rho, int precisi
   for (int l = 0; l < nlev; ++l) st->rho[l] = rho[l];
   st->precision = precision;
   st->store = store ? 1 : 0;
-  int lk = precision == GF_MIXED ? GF_LINK32 : GF_LINK64;
-  int mk = precision == GF_MIXED ? GF_MAT32 : GF_MAT64;
+  // double-float stacks keep their levels and adjoint fields as fp32 hi/lo
+  // pairs (no conversion on the kernels' loads)
+  int lk = precision == GF_MIXED ? GF_LINK32 : (precision == GF_PREC_DF ? GF_LINKDF : GF_LINK64);
+  int mk = precision == GF_MIXED ? GF_MAT32 : (precision == GF_PREC_DF ? GF_MATDF : GF_MAT64);
   try {
     for (int l = 1; l <= nlev; ++l) {
       if (fwd_only && arena && l <= 2) {
@@ -470,6 +488,18 @@ extern "C" int gf_stout_backward(gf_ctx* ctx, gf_stout* st, const gf_field* dSdU
   need_ctx(ctx, dSdUbar);
   need_ctx(ctx, dSdU);
   stout_backward(ctx, st, dSdUbar, 0.0, dSdU, nullptr, 0.0);
+  API_END(ctx)
+}
+
+extern "C" int gf_stout_param_derivatives(gf_ctx* ctx, gf_stout* st, const gf_field* U, const gf_field* dSdUbar,
+                                          double* dSdrho) {
+  API_BEGIN
+  need(ctx && st && U && dSdUbar && dSdrho, "gf_stout_param_derivatives: null argument");
+  need_ctx(ctx, U);
+  need_ctx(ctx, dSdUbar);
+  need(st->ctx == ctx, "gf_stout_param_derivatives: stack belongs to another context");
+  stout_forward(ctx, st, U, nullptr);
+  stout_backward(ctx, st, dSdUbar, 0.0, nullptr, nullptr, 0.0, dSdrho);
   API_END(ctx)
 }
 

@@ -14,6 +14,8 @@ size_t field_bytes(const Geom& g, int kind) {
   switch (kind) {
     case GF_LINK64:
     case GF_MAT64: return 4 * 9 * V * sizeof(double2);
+    case GF_LINKDF:
+    case GF_MATDF: return 4 * 9 * V * sizeof(float4);
     case GF_LINK32: return 4 * 3 * V * sizeof(float4);
     case GF_MAT32: return 4 * 9 * V * sizeof(float2);
     case GF_MOM64: return 4 * 8 * V * sizeof(double);
@@ -145,7 +147,8 @@ __global__ void k_hash(const unsigned long long* __restrict__ w, size_t n, unsig
 
 unsigned long long field_hash(gf_ctx* ctx, const gf_field* f) {
   GF_CUDA(cudaMemsetAsync(ctx->d_hash, 0, sizeof(unsigned long long), ctx->stream));
-  k_hash<<<152 * 8, 256, 0, ctx->stream>>>((const unsigned long long*)f->ptr, f->bytes / 8, ctx->d_hash);
+  // a grid-stride loop over the field: eight blocks of 256 threads per SM
+  k_hash<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>((const unsigned long long*)f->ptr, f->bytes / 8, ctx->d_hash);
   GF_CHECK_LAUNCH();
   GF_CUDA(cudaMemcpyAsync(ctx->h_hash, ctx->d_hash, sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
   GF_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -474,11 +477,29 @@ void link64_to_32(gf_ctx* ctx, gf_field* dst, const gf_field* src) {
   GF_CHECK_LAUNCH();
 }
 
+// fp64 <-> double-float-native storage, one complex element per thread
+__global__ void k_f64_to_dfn(const double2* __restrict__ in, float4* __restrict__ out, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double2 v = in[i];
+  const dfl re = df_from_double(v.x), im = df_from_double(v.y);
+  out[i] = make_float4(re.hi, re.lo, im.hi, im.lo);
+}
+__global__ void k_dfn_to_f64(const float4* __restrict__ in, double2* __restrict__ out, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 v = in[i];
+  out[i] = make_double2(df_to_double(dfl(v.x, v.y)), df_to_double(dfl(v.z, v.w)));
+}
+
+static bool is_f64_full(int k) { return k == GF_LINK64 || k == GF_MAT64; }
+static bool is_dfn(int k) { return k == GF_LINKDF || k == GF_MATDF; }
+
 void copy_field(gf_ctx* ctx, gf_field* dst, const gf_field* src) {
   if (!dst || !src) throw gf_error(GF_EINVAL, "copy: null field");
   if (dst == src) return;
   int a = src->kind, b = dst->kind;
-  bool full64 = (a == GF_LINK64 || a == GF_MAT64) && (b == GF_LINK64 || b == GF_MAT64);
+  bool full64 = (is_f64_full(a) && is_f64_full(b)) || (is_dfn(a) && is_dfn(b));
   if (a == b || full64) {
     GF_CUDA(cudaMemcpyAsync(dst->ptr, src->ptr, src->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
     return;
@@ -494,6 +515,10 @@ void copy_field(gf_ctx* ctx, gf_field* dst, const gf_field* src) {
     k_mat64_to_32<<<nb, 256, 0, ctx->stream>>>((const double2*)src->ptr, (float2*)dst->ptr, n);
   } else if (a == GF_MAT32 && (b == GF_MAT64 || b == GF_LINK64)) {
     k_mat32_to_64<<<nb, 256, 0, ctx->stream>>>((const float2*)src->ptr, (double2*)dst->ptr, n);
+  } else if (is_f64_full(a) && is_dfn(b)) {
+    k_f64_to_dfn<<<nb, 256, 0, ctx->stream>>>((const double2*)src->ptr, (float4*)dst->ptr, n);
+  } else if (is_dfn(a) && is_f64_full(b)) {
+    k_dfn_to_f64<<<nb, 256, 0, ctx->stream>>>((const float4*)src->ptr, (double2*)dst->ptr, n);
   } else {
     throw gf_error(GF_EINVAL, "copy: unsupported kind conversion " + std::to_string(a) + " -> " + std::to_string(b));
   }
@@ -513,6 +538,11 @@ __global__ void k_scale(double* __restrict__ y, double a, size_t n) {
 
 void mom_axpy(gf_ctx* ctx, gf_field* y, double a, const gf_field* x) {
   size_t n = (size_t)32 * ctx->geom.vol;
+  k_axpy<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>((double*)y->ptr, a, (const double*)x->ptr, n);
+  GF_CHECK_LAUNCH();
+}
+void field_axpy(gf_ctx* ctx, gf_field* y, double a, const gf_field* x) {
+  size_t n = y->bytes / sizeof(double);
   k_axpy<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>((double*)y->ptr, a, (const double*)x->ptr, n);
   GF_CHECK_LAUNCH();
 }

@@ -33,9 +33,16 @@ void count_launch();
 
 #define GF_PROF_CAP 4096
 
-// Stack precision with fp64 storage and double-float arithmetic: the
-// GF_DFLOAT form, and the Hamiltonian of the mixed form (forward only).
+// Stack precision with double-float arithmetic: the GF_DFLOAT form, and the
+// Hamiltonian of the mixed form (forward only).
 #define GF_PREC_DF GF_DFLOAT
+
+// Internal field kinds of double-float stacks: 18-real links and general
+// matrices stored as fp32 hi/lo pairs (one float4 per complex element, the
+// size of GF_LINK64). They never cross the C-ABI: the API converts at the
+// boundary.
+#define GF_LINKDF 101
+#define GF_MATDF 102
 
 struct gf_field {
   gf_ctx* ctx;
@@ -47,6 +54,7 @@ struct gf_field {
 
 struct gf_ctx {
   int device;
+  int sm_count;  // streaming multiprocessors of the device (grid sizing)
   gf::Geom geom;
   cudaStream_t stream;
   int own_stream;
@@ -152,6 +160,7 @@ void gaussian_momenta(gf_ctx* ctx, gf_field* P, uint64_t seed, uint64_t sweep);
 void copy_field(gf_ctx* ctx, gf_field* dst, const gf_field* src);
 void zero_field(gf_ctx* ctx, gf_field* f);
 void mom_axpy(gf_ctx* ctx, gf_field* y, double a, const gf_field* x);  // y += a x
+void field_axpy(gf_ctx* ctx, gf_field* y, double a, const gf_field* x);  // y += a x, fp64 fields of one kind
 void mom_scale(gf_ctx* ctx, gf_field* y, double a);                      // y *= a
 
 // ---- Wilson action pieces (gf_wilson.cu) ----
@@ -182,8 +191,9 @@ void stout_forward(gf_ctx* ctx, gf_stout* st, const gf_field* U, gf_field* Uout)
 // derivative is taken from the Wilson action (coefficient beta/2 per staple)
 // on the smeared links. If P is non-null the thin-link result is turned into
 // the MD force and added as P += eps * F; otherwise it is written to dSdU.
+// dsdrho (optional, nlev entries): dS/drho of every level
 void stout_backward(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, double beta, gf_field* dSdU,
-                    gf_field* P, double eps);
+                    gf_field* P, double eps, double* dsdrho = nullptr);
 const gf_field* stout_top(const gf_stout* st);
 
 // ---- flow (gf_flow.cu) ----

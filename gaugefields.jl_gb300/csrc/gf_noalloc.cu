@@ -20,7 +20,10 @@
 // In host code the array's name is only a host-side stand-in; the device
 // address is looked up with cudaGetSymbolAddress once per device, with that
 // device current, by the first call on the device. That first call should be
-// made before any stream capture begins.
+// made before any stream capture begins. The address is kept for the life of
+// the process: after cudaDeviceReset (or any teardown of the device's primary
+// context) the kept address is stale, so this entry point must not be called
+// again in a process that has reset the device.
 #include "gf_internal.h"
 #include "stencil.cuh"
 #include <mutex>
@@ -87,17 +90,20 @@ static int noalloc_fail(int code, const std::string& m) {
 extern "C" int gf_plaquette_noalloc(const void* links, const int L[4], double* out, void* stream) {
   using namespace gf;
   if (!links || !L || !out) return noalloc_fail(GF_EINVAL, "gf_plaquette_noalloc: null argument");
+  // The volume is checked against the limit after every factor, so the
+  // product never overflows (each extent is below 2^31 and the running
+  // product at most 2^24 before the next multiply).
+  const long long vmax = (long long)GF_NOALLOC_MAX_BLOCKS * GF_NOALLOC_BLOCK;
   long long V = 1;
   for (int i = 0; i < 4; ++i) {
     if (L[i] < 2 || (L[i] % 2) != 0)
       return noalloc_fail(GF_EINVAL, "gf_plaquette_noalloc: every lattice extent must be even and >= 2");
     V *= L[i];
+    if (V > vmax)
+      return noalloc_fail(GF_EINVAL, "gf_plaquette_noalloc: lattice has more than " + std::to_string(vmax) +
+                                         " sites; the fixed scratch holds at most " + std::to_string(vmax));
   }
   long long nb = (V + GF_NOALLOC_BLOCK - 1) / GF_NOALLOC_BLOCK;
-  if (nb > GF_NOALLOC_MAX_BLOCKS)
-    return noalloc_fail(GF_EINVAL, "gf_plaquette_noalloc: lattice has " + std::to_string(V) +
-                                       " sites; the fixed scratch holds at most " +
-                                       std::to_string((long long)GF_NOALLOC_MAX_BLOCKS * GF_NOALLOC_BLOCK));
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return noalloc_fail(GF_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));

@@ -51,20 +51,6 @@ struct Prec<float> {
   }
 };
 
-// fp64 storage, double-float arithmetic (the GF_DFLOAT form; the mixed
-// form's Hamiltonian smears in this precision)
-template <>
-struct Prec<dfl> {
-  typedef LinkSrc<dfl, false> Src;
-  typedef double2 LinkElem;
-  typedef double2 MatElem;
-  static constexpr int link_kind = GF_LINK64;
-  static constexpr int mat_kind = GF_MAT64;
-  static __device__ __forceinline__ void store_link(double2* p, int mu, int s, int V, const mat3<dfl>& m) {
-    LinkFull<dfl>::store(p, mu, s, V, m);
-  }
-};
-
 // i * r * A  (elementwise)
 template <typename R>
 __device__ __forceinline__ mat3<R> times_i(R r, const mat3<R>& a) {
@@ -247,6 +233,12 @@ __global__ void __launch_bounds__(128, GF_MINB_ADJ(R))
 // the results are the same. Out-of-line forms of the product were slower (argument passing) or
 // miscompiled (pointers into the caller's registers), which this avoids.
 // --------------------------------------------------------------------------
+// Products of the table kernels: the fixed-grid form (dfg_matmul, six fp32
+// operations per term) or the TwoSum-based one (df_matmul, twelve).
+#ifndef GF_DF_GRID
+#define GF_DF_GRID 1
+#endif
+
 struct DfOp {
   // src: 0, 1, 2 fields F0, F1, F2, 3 + k slot k; dir: 0 the kernel's link
   // direction, 1 the loop axis; site: index into the kernel's five sites
@@ -282,23 +274,37 @@ struct DfSites {
 __device__ __forceinline__ int pick_site(const DfSites& st, int i) {
   return i == 0 ? st.x[0] : i == 1 ? st.x[1] : i == 2 ? st.x[2] : i == 3 ? st.x[3] : st.x[4];
 }
+// The operand fields of a table kernel: F0 in storage E0 (fp64 for the
+// level-0 forward of a forward-only stack, which reads the thin links in
+// place), F1 and F2 double-float-native.
+template <typename E0>
 struct DfFields {
-  const double2* f[3];
+  const E0* f0;
+  const float4* f1;
+  const float4* f2;
 };
+template <typename E0>
 __device__ __forceinline__ mat3<dfl> df_operand(int src, int dir, int site, int dagger, const float* sm, int tid,
-                                                const DfFields& F, int V, int d0, int d1, const DfSites& st) {
+                                                const DfFields<E0>& F, int V, int d0, int d1, const DfSites& st) {
   mat3<dfl> m;
+  const int mu = dir ? d1 : d0, x = pick_site(st, site);
   if (src >= 3) m = slot_load(sm, src - 3, tid);
-  else m = LinkFull<dfl>::load(src == 0 ? F.f[0] : src == 1 ? F.f[1] : F.f[2], dir ? d1 : d0, pick_site(st, site), V);
+  else if (src == 0) m = DfIO<E0>::load(F.f0, mu, x, V);
+  else m = LinkDfn::load(src == 1 ? F.f1 : F.f2, mu, x, V);
   if (dagger) m = dag(m);
   return m;
 }
-__device__ __forceinline__ void df_exec(const DfOp op, float* sm, int tid, const DfFields& F, int V, int d0, int d1,
-                                        const DfSites& st) {
+template <typename E0>
+__device__ __forceinline__ void df_exec(const DfOp op, float* sm, int tid, const DfFields<E0>& F, int V, int d0,
+                                        int d1, const DfSites& st) {
   const mat3<dfl> A = df_operand(op.a_src, op.a_dir, op.a_site, op.a_dag, sm, tid, F, V, d0, d1, st);
   const mat3<dfl> B = df_operand(op.b_src, op.b_dir, op.b_site, op.b_dag, sm, tid, F, V, d0, d1, st);
   const mat3<dfl> C = op.accumulate ? slot_load(sm, op.out, tid) : zero3<dfl>();
+#if GF_DF_GRID
+  slot_store(sm, op.out, tid, dfg_matmul<false, false, true>(A, B, &C));
+#else
   slot_store(sm, op.out, tid, df_matmul<false, false, true>(A, B, &C));
+#endif
 }
 
 // The gather: F0 = U, F1 = Z, d0 = nu, d1 = kappa; sites x, x+nu, x+kappa,
@@ -321,10 +327,10 @@ __constant__ DfOp c_gather_ops[10] = {
 #ifndef GF_DF_GATHER_MINB
 #define GF_DF_GATHER_MINB 3
 #endif
-template <bool FORCE>
+template <bool FORCE, typename EOUT>
 __global__ void __launch_bounds__(128, GF_DF_GATHER_MINB)
-    k_bwd_gather_df(const double2* __restrict__ U, const double2* __restrict__ Z, const double2* __restrict__ Dp,
-                    double2* __restrict__ Dout, double* __restrict__ P, Geom g, dfl rho, double coef) {
+    k_bwd_gather_df(const float4* __restrict__ U, const float4* __restrict__ Z, const float4* __restrict__ Dp,
+                    EOUT* __restrict__ Dout, double* __restrict__ P, Geom g, dfl rho, double coef) {
   __shared__ float sm[2 * 36 * 128];
   const int tid = threadIdx.x;
   int s, nu;
@@ -344,20 +350,20 @@ __global__ void __launch_bounds__(128, GF_DF_GATHER_MINB)
     ss.x[3] = nbr_rt(g, st, K, -1);
     ss.x[4] = nbr2_rt(g, st, K, -1, nu, +1);
 #pragma unroll 1
-    for (int q = 0; q < 10; ++q) df_exec(c_gather_ops[q], sm, tid, DfFields{{U, Z, Z}}, V, nu, K, ss);
+    for (int q = 0; q < 10; ++q) df_exec(c_gather_ops[q], sm, tid, DfFields<float4>{U, Z, Z}, V, nu, K, ss);
   }
   if (!live) return;
-  mat3<dfl> d = LinkFull<dfl>::load(Dp, nu, s, V);
+  mat3<dfl> d = LinkDfn::load(Dp, nu, s, V);
   axpy_to(d, rho, slot_load(sm, 1, tid));
   if (FORCE) {
-    const mat3<dfl> M = mul_nn(LinkFull<dfl>::load(U, nu, s, V), d);
+    const mat3<dfl> M = mul_nn(LinkDfn::load(U, nu, s, V), d);
     dfl c[8];
     ta_coeffs(M, c);
     double* p = P + (size_t)nu * 8 * V + s;
 #pragma unroll
     for (int a = 0; a < 8; ++a) p[(size_t)a * V] += coef * to_f64(c[a]);
   } else {
-    LinkFull<dfl>::store(Dout, nu, s, V, d);
+    DfIO<EOUT>::store(Dout, nu, s, V, d);
   }
 }
 
@@ -378,8 +384,9 @@ __constant__ DfOp c_stout_ops[6] = {
 #ifndef GF_DF_FWD_MINB
 #define GF_DF_FWD_MINB 3
 #endif
+template <typename EIN>
 __global__ void __launch_bounds__(128, GF_DF_FWD_MINB)
-    k_stout_fwd_df(const double2* __restrict__ U, double2* __restrict__ Uout, double2* __restrict__ Cout, Geom g,
+    k_stout_fwd_df(const EIN* __restrict__ U, float4* __restrict__ Uout, float4* __restrict__ Cout, Geom g,
                    dfl rho) {
   __shared__ float sm[2 * 36 * 128];
   const int tid = threadIdx.x;
@@ -406,11 +413,11 @@ __global__ void __launch_bounds__(128, GF_DF_FWD_MINB)
       // Q = TA(rho S^dag U^dag) = -rho TA(U S): exp(Q) = exp(i Qh), Qh = i rho TA(U S)
       const mat3<dfl> qh = times_i(rho, ta_proj(slot_load(sm, 0, tid)));
       slot_store(sm, 0, tid, expiq(qh));
-      if (Cout && live) LinkFull<dfl>::store(Cout, mu, s, V, scale(rho, dag(slot_load(sm, 1, tid))));
+      if (Cout && live) LinkDfn::store(Cout, mu, s, V, scale(rho, dag(slot_load(sm, 1, tid))));
     }
-    df_exec(c_stout_ops[q < 12 ? (q & 3) : q - 8], sm, tid, DfFields{{U, U, U}}, V, mu, nu, ss);
+    df_exec(c_stout_ops[q < 12 ? (q & 3) : q - 8], sm, tid, DfFields<EIN>{U, nullptr, nullptr}, V, mu, nu, ss);
   }
-  if (live) LinkFull<dfl>::store(Uout, mu, s, V, slot_load(sm, 1, tid));
+  if (live) LinkDfn::store(Uout, mu, s, V, slot_load(sm, 1, tid));
 }
 
 // The local adjoint: F0 = U, F1 = Dbar (or the top level's smeared links),
@@ -445,8 +452,8 @@ __constant__ DfOp c_local_ops[31] = {
 
 template <bool TOP>
 __global__ void __launch_bounds__(128, GF_MINB_ADJ(dfl))
-    k_bwd_local_df(const double2* __restrict__ U, const double2* __restrict__ F1, const double2* __restrict__ Cst,
-                   double2* __restrict__ Zout, double2* __restrict__ Dpout, Geom g, dfl rho, dfl halfbeta) {
+    k_bwd_local_df(const float4* __restrict__ U, const float4* __restrict__ F1, const float4* __restrict__ Cst,
+                   float4* __restrict__ Zout, float4* __restrict__ Dpout, Geom g, dfl rho, dfl halfbeta) {
   extern __shared__ float sm[];  // GF_LOCAL_SLOTS slots of 36 x 128 floats
   const int tid = threadIdx.x;
   int s, mu;
@@ -456,7 +463,7 @@ __global__ void __launch_bounds__(128, GF_MINB_ADJ(dfl))
   const int sc = live ? s : 0;
   const Site st = site_of(g, sc);
   const bool recompute = Cst == nullptr;
-  const DfFields F{{U, F1, Cst ? Cst : U}};
+  const DfFields<float4> F{U, F1, Cst ? Cst : U};
   DfSites ss;
   ss.x[0] = sc;
   ss.x[1] = nbr_rt(g, st, mu, +1);
@@ -517,21 +524,63 @@ __global__ void __launch_bounds__(128, GF_MINB_ADJ(dfl))
       slot_store(sm, 0, tid, ta_proj(times_i(dfl(-1), gam)));  // Y
       slot_store(sm, 2, tid, E);                                // e^Q
     }
-    if (q == 28 && live) LinkFull<dfl>::store(Zout, mu, s, V, slot_load(sm, 3, tid));
+    if (q == 28 && live) LinkDfn::store(Zout, mu, s, V, slot_load(sm, 3, tid));
   }
-  if (live) LinkFull<dfl>::store(Dpout, mu, s, V, slot_load(sm, 3, tid));
+  if (live) LinkDfn::store(Dpout, mu, s, V, slot_load(sm, 3, tid));
 }
 
-#ifndef GF_DF_LOCAL_LOOP
-#define GF_DF_LOCAL_LOOP 1
-#endif
+// --------------------------------------------------------------------------
+// dS/drho of one level (parameter_derivatives, the rho part of
+// backward_dSdUαUβρ_add!, src/smearing/stout_fast.jl:371-386). With
+// C = rho S^dag and Z = dS/dC from the level's local adjoint,
+//   dS/drho = 2 Re sum_{x,mu} tr(Z_mu(x) S_mu(x)^dag),
+// S recomputed from the level input (valid at rho = 0 too). One partial sum
+// per block (deterministic two-stage reduction).
+// --------------------------------------------------------------------------
+template <typename R, class SRC, class ZL>
+__global__ void __launch_bounds__(128) k_dsdrho(SRC U, ZL Z, Geom g, double* __restrict__ part) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  double v = 0.0;
+  if (s < g.vol) {
+    const Site st = site_of(g, s);
+#pragma unroll 1
+    for (int mu = 0; mu < 4; ++mu) {
+      const mat3<R> S = staple_sum<R>(mu, U, g, st, s);
+      const mat3<R> z = Z(mu, s, g.vol);
+      R t = R(0);
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) t += z.e[i][j].re * S.e[i][j].re + z.e[i][j].im * S.e[i][j].im;
+      v += 2.0 * (double)t;
+    }
+  }
+  block_partial_sum(v, part);
+}
 
-#ifndef GF_DF_GATHER_LOOP
-#define GF_DF_GATHER_LOOP 1
-#endif
-#ifndef GF_DF_FWD_LOOP
-#define GF_DF_FWD_LOOP 1
-#endif
+// dS/drho of level `l` from the stack's Z (after that level's local adjoint)
+static double level_dsdrho(gf_ctx* ctx, gf_stout* st, int l) {
+  const int nb = blocks_for(ctx->geom.vol, 128);
+  const gf_field* u = st->lev_in[l];
+  if (st->precision == GF_FP64) {
+    k_dsdrho<double><<<nb, 128, 0, ctx->stream>>>(LinkSrc<double, false>{(const double2*)u->ptr},
+                                                  LinkSrc<double, false>{(const double2*)st->Z->ptr}, ctx->geom,
+                                                  ctx->d_partials);
+  } else if (st->precision == GF_MIXED) {
+    k_dsdrho<float><<<nb, 128, 0, ctx->stream>>>(LinkSrc<float, true>{(const float4*)u->ptr},
+                                                 LinkSrc<float, false>{(const float2*)st->Z->ptr}, ctx->geom,
+                                                 ctx->d_partials);
+  } else if (u->kind == GF_LINKDF) {
+    // double-float stack: fp64 arithmetic on hi + lo
+    k_dsdrho<double><<<nb, 128, 0, ctx->stream>>>(LinkSrcDfn64{(const float4*)u->ptr},
+                                                  LinkSrcDfn64{(const float4*)st->Z->ptr}, ctx->geom,
+                                                  ctx->d_partials);
+  } else {
+    throw gf_error(GF_EINVAL, "dS/drho: unexpected level storage");
+  }
+  GF_CHECK_LAUNCH();
+  return finish_reduction(ctx, nb);
+}
 
 // --------------------------------------------------------------------------
 // host drivers
@@ -554,23 +603,38 @@ static void forward_impl(gf_ctx* ctx, gf_stout* st) {
   dim3 grid = stencil_grid(ctx->geom.vol, 128);
   for (int l = 0; l < st->nlev; ++l) {
     ProfScope prof(ctx, kclass<R>(GF_K_STOUT_FWD, GF_K_STOUT_FWD64, GF_K_STOUT_FWD_DF));
-    if constexpr (GF_DF_FWD_LOOP && std::is_same<R, dfl>::value) {
-      k_stout_fwd_df<<<grid, 128, 0, ctx->stream>>>((const double2*)st->lev_in[l]->ptr,
-                                                    (double2*)st->lev_in[l + 1]->ptr,
-                                                    st->store ? (double2*)st->C[l]->ptr : nullptr, ctx->geom,
-                                                    (R)st->rho[l]);
-      GF_CHECK_LAUNCH();
-      continue;
+    if constexpr (std::is_same<R, dfl>::value) {
+      // double-float stacks store every level natively; level 0 of a
+      // forward-only stack is the fp64 thin links, read in place
+      float4* cout = st->store ? (float4*)st->C[l]->ptr : nullptr;
+      float4* uout = (float4*)st->lev_in[l + 1]->ptr;
+      if (st->lev_in[l]->kind == GF_LINK64)
+        k_stout_fwd_df<double2><<<grid, 128, 0, ctx->stream>>>((const double2*)st->lev_in[l]->ptr, uout, cout,
+                                                               ctx->geom, (R)st->rho[l]);
+      else
+        k_stout_fwd_df<float4><<<grid, 128, 0, ctx->stream>>>((const float4*)st->lev_in[l]->ptr, uout, cout,
+                                                              ctx->geom, (R)st->rho[l]);
+    } else {
+      k_stout_fwd<R><<<grid, 128, 0, ctx->stream>>>(
+          src_of<R>(st->lev_in[l]), (typename Prec<R>::LinkElem*)st->lev_in[l + 1]->ptr,
+          st->store ? (typename Prec<R>::MatElem*)st->C[l]->ptr : nullptr, ctx->geom, (R)st->rho[l]);
     }
-    k_stout_fwd<R><<<grid, 128, 0, ctx->stream>>>(
-        src_of<R>(st->lev_in[l]), (typename Prec<R>::LinkElem*)st->lev_in[l + 1]->ptr,
-        st->store ? (typename Prec<R>::MatElem*)st->C[l]->ptr : nullptr, ctx->geom, (R)st->rho[l]);
     GF_CHECK_LAUNCH();
   }
 }
 
+// Kind of a stack's level-0 input: fp32 12-real (mixed), double-float-native
+// (a double-float stack with an adjoint keeps its own copy of the thin
+// links), or the caller's fp64 links (plain form; forward-only double-float
+// stacks read them in place).
+static int level0_kind(const gf_stout* st) {
+  if (st->precision == GF_MIXED) return GF_LINK32;
+  if (st->precision == GF_PREC_DF && !st->fwd_only) return GF_LINKDF;
+  return GF_LINK64;
+}
+
 void stout_forward(gf_ctx* ctx, gf_stout* st, const gf_field* U, gf_field* Uout) {
-  int lk = st->precision == GF_MIXED ? GF_LINK32 : GF_LINK64;
+  const int lk = level0_kind(st);
   gf_field* old = st->lev_in[0];
   if (U->kind == lk) {
     // alias the caller's thin links (not owned by the stack)
@@ -578,10 +642,10 @@ void stout_forward(gf_ctx* ctx, gf_stout* st, const gf_field* U, gf_field* Uout)
     a->owned = 0;
     st->lev_in[0] = a;
     field_delete(old);  // frees storage only if the old entry was owned
-  } else if (st->precision == GF_MIXED && U->kind == GF_LINK64) {
-    // mixed stack fed with fp64 links: keep an owned fp32 12-real thin copy
+  } else if ((lk == GF_LINK32 || lk == GF_LINKDF) && U->kind == GF_LINK64) {
+    // keep an owned copy of the fp64 thin links in the stack's storage
     if (!old || !old->owned) {
-      st->lev_in[0] = field_new(ctx, GF_LINK32);
+      st->lev_in[0] = field_new(ctx, lk);
       field_delete(old);
     }
     copy_field(ctx, st->lev_in[0], U);
@@ -597,9 +661,57 @@ void stout_forward(gf_ctx* ctx, gf_stout* st, const gf_field* U, gf_field* Uout)
 
 const gf_field* stout_top(const gf_stout* st) { return st->lev_in[st->nlev]; }
 
+// Double-float adjoint on native storage. A caller's dS/dUbar (fp64) is
+// converted into D[1] first: the top level's local kernel reads it before
+// that level's gather overwrites D[1]. A caller's dS/dU receives the bottom
+// gather's output in fp64.
+static void backward_df(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, double beta, gf_field* dSdU,
+                        gf_field* P, double eps, double* dsdrho) {
+  dim3 grid = stencil_grid(ctx->geom.vol, 128);
+  const float4* dbar = nullptr;
+  if (dSdUbar) {
+    copy_field(ctx, st->D[1], dSdUbar);
+    dbar = (const float4*)st->D[1]->ptr;
+  }
+  int cur = 0;
+  for (int l = st->nlev - 1; l >= 0; --l) {
+    const bool top = (l == st->nlev - 1) && dSdUbar == nullptr;
+    const float4* Cst = st->store ? (const float4*)st->C[l]->ptr : nullptr;
+    const float4* din = (l == st->nlev - 1) ? dbar : (const float4*)st->D[cur]->ptr;
+    const float4* u = (const float4*)st->lev_in[l]->ptr;
+    {
+      ProfScope prof(ctx, GF_K_BWD_LOCAL_DF);
+      const size_t smem = (size_t)GF_LOCAL_SLOTS * 36 * 128 * sizeof(float);
+      auto kern = top ? k_bwd_local_df<true> : k_bwd_local_df<false>;
+      GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      kern<<<grid, 128, smem, ctx->stream>>>(u, top ? (const float4*)st->lev_in[l + 1]->ptr : din, Cst,
+                                             (float4*)st->Z->ptr, (float4*)st->Dp->ptr, ctx->geom, (dfl)st->rho[l],
+                                             (dfl)(0.5 * beta));
+      GF_CHECK_LAUNCH();
+    }
+    if (dsdrho) dsdrho[l] = level_dsdrho(ctx, st, l);
+    const int nxt = cur ^ 1;
+    ProfScope prof(ctx, GF_K_BWD_GATHER_DF);
+    const float4* z = (const float4*)st->Z->ptr;
+    const float4* dp = (const float4*)st->Dp->ptr;
+    if (l == 0 && P) {
+      k_bwd_gather_df<true, float4><<<grid, 128, 0, ctx->stream>>>(u, z, dp, nullptr, (double*)P->ptr, ctx->geom,
+                                                                   (dfl)st->rho[0], -eps / 3.0);
+    } else if (l == 0 && dSdU) {
+      k_bwd_gather_df<false, double2><<<grid, 128, 0, ctx->stream>>>(u, z, dp, (double2*)dSdU->ptr, nullptr,
+                                                                     ctx->geom, (dfl)st->rho[0], 0.0);
+    } else {
+      k_bwd_gather_df<false, float4><<<grid, 128, 0, ctx->stream>>>(u, z, dp, (float4*)st->D[nxt]->ptr, nullptr,
+                                                                    ctx->geom, (dfl)st->rho[l], 0.0);
+    }
+    GF_CHECK_LAUNCH();
+    cur = nxt;
+  }
+}
+
 template <typename R>
 static void backward_impl(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, double beta, gf_field* dSdU,
-                          gf_field* P, double eps) {
+                          gf_field* P, double eps, double* dsdrho) {
   dim3 grid = stencil_grid(ctx->geom.vol, 128);
   typedef typename Prec<R>::MatElem ME;
   const ME* dbar = dSdUbar ? (const ME*)dSdUbar->ptr : nullptr;
@@ -609,50 +721,27 @@ static void backward_impl(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, do
     const ME* Cst = st->store ? (const ME*)st->C[l]->ptr : nullptr;
     const ME* din = (l == st->nlev - 1) ? dbar : (const ME*)st->D[cur]->ptr;
     {
-    ProfScope prof(ctx, kclass<R>(GF_K_BWD_LOCAL, GF_K_BWD_LOCAL64, GF_K_BWD_LOCAL_DF));
-    if constexpr (GF_DF_LOCAL_LOOP && std::is_same<R, dfl>::value) {
-      const size_t smem = (size_t)GF_LOCAL_SLOTS * 36 * 128 * sizeof(float);
-      auto kern = top ? k_bwd_local_df<true> : k_bwd_local_df<false>;
-      GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      kern<<<grid, 128, smem, ctx->stream>>>((const double2*)st->lev_in[l]->ptr,
-                                             top ? (const double2*)st->lev_in[l + 1]->ptr : (const double2*)din,
-                                             (const double2*)Cst, (double2*)st->Z->ptr, (double2*)st->Dp->ptr,
-                                             ctx->geom, (R)st->rho[l], (R)(0.5 * beta));
-    } else if (top) {
-      k_bwd_local<R, true><<<grid, 128, 0, ctx->stream>>>(src_of<R>(st->lev_in[l]), src_of<R>(st->lev_in[l + 1]),
-                                                          nullptr, Cst, (ME*)st->Z->ptr, (ME*)st->Dp->ptr, ctx->geom,
-                                                          (R)st->rho[l], (R)(0.5 * beta));
-    } else {
-      k_bwd_local<R, false><<<grid, 128, 0, ctx->stream>>>(src_of<R>(st->lev_in[l]), src_of<R>(st->lev_in[l + 1]),
-                                                           din, Cst, (ME*)st->Z->ptr, (ME*)st->Dp->ptr, ctx->geom,
-                                                           (R)st->rho[l], (R)(0.5 * beta));
-    }
-    GF_CHECK_LAUNCH();
-    }
-    int nxt = cur ^ 1;
-    ProfScope prof(ctx, kclass<R>(GF_K_BWD_GATHER, GF_K_BWD_GATHER64, GF_K_BWD_GATHER_DF));
-    if constexpr (GF_DF_GATHER_LOOP && std::is_same<R, dfl>::value) {
-      const double2* u = (const double2*)st->lev_in[l]->ptr;
-      if (l == 0 && P) {
-        k_bwd_gather_df<true><<<grid, 128, 0, ctx->stream>>>(u, (const double2*)st->Z->ptr, (const double2*)st->Dp->ptr,
-                                                             nullptr, (double*)P->ptr, ctx->geom, (R)st->rho[0],
-                                                             -eps / 3.0);
+      ProfScope prof(ctx, kclass<R>(GF_K_BWD_LOCAL, GF_K_BWD_LOCAL64, GF_K_BWD_LOCAL_DF));
+      if (top) {
+        k_bwd_local<R, true><<<grid, 128, 0, ctx->stream>>>(src_of<R>(st->lev_in[l]), src_of<R>(st->lev_in[l + 1]),
+                                                            nullptr, Cst, (ME*)st->Z->ptr, (ME*)st->Dp->ptr,
+                                                            ctx->geom, (R)st->rho[l], (R)(0.5 * beta));
       } else {
-        double2* out = (l == 0) ? (double2*)dSdU->ptr : (double2*)st->D[nxt]->ptr;
-        k_bwd_gather_df<false><<<grid, 128, 0, ctx->stream>>>(u, (const double2*)st->Z->ptr,
-                                                              (const double2*)st->Dp->ptr, out, nullptr, ctx->geom,
-                                                              (R)st->rho[l], 0.0);
+        k_bwd_local<R, false><<<grid, 128, 0, ctx->stream>>>(src_of<R>(st->lev_in[l]), src_of<R>(st->lev_in[l + 1]),
+                                                             din, Cst, (ME*)st->Z->ptr, (ME*)st->Dp->ptr, ctx->geom,
+                                                             (R)st->rho[l], (R)(0.5 * beta));
       }
       GF_CHECK_LAUNCH();
-      cur = nxt;
-      continue;
     }
+    if (dsdrho) dsdrho[l] = level_dsdrho(ctx, st, l);
+    int nxt = cur ^ 1;
+    ProfScope prof(ctx, kclass<R>(GF_K_BWD_GATHER, GF_K_BWD_GATHER64, GF_K_BWD_GATHER_DF));
     if (l == 0 && P) {
       k_bwd_gather<R, true><<<grid, 128, 0, ctx->stream>>>(src_of<R>(st->lev_in[0]), (const ME*)st->Z->ptr,
                                                            (const ME*)st->Dp->ptr, nullptr, (double*)P->ptr,
                                                            ctx->geom, (R)st->rho[0], -eps / 3.0);
     } else {
-      ME* out = (l == 0) ? (ME*)dSdU->ptr : (ME*)st->D[nxt]->ptr;
+      ME* out = (l == 0 && dSdU) ? (ME*)dSdU->ptr : (ME*)st->D[nxt]->ptr;
       k_bwd_gather<R, false><<<grid, 128, 0, ctx->stream>>>(src_of<R>(st->lev_in[l]), (const ME*)st->Z->ptr,
                                                             (const ME*)st->Dp->ptr, out, nullptr, ctx->geom,
                                                             (R)st->rho[l], 0.0);
@@ -663,16 +752,18 @@ static void backward_impl(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, do
 }
 
 void stout_backward(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, double beta, gf_field* dSdU, gf_field* P,
-                    double eps) {
+                    double eps, double* dsdrho) {
   if (!st->have_forward) throw gf_error(GF_ESTATE, "stout backward called before forward");
   if (st->fwd_only) throw gf_error(GF_EINVAL, "stout backward: forward-only stack");
   if (st->nlev < 1) throw gf_error(GF_EINVAL, "stout backward needs at least one level");
   int mk = st->precision == GF_MIXED ? GF_MAT32 : GF_MAT64;
   if (dSdUbar && dSdUbar->kind != mk) throw gf_error(GF_EINVAL, "stout backward: dS/dUbar kind does not match the stack precision");
-  if (!P && (!dSdU || dSdU->kind != mk)) throw gf_error(GF_EINVAL, "stout backward: dS/dU kind does not match the stack precision");
-  if (st->precision == GF_FP64) backward_impl<double>(ctx, st, dSdUbar, beta, dSdU, P, eps);
-  else if (st->precision == GF_PREC_DF) backward_impl<dfl>(ctx, st, dSdUbar, beta, dSdU, P, eps);
-  else backward_impl<float>(ctx, st, dSdUbar, beta, dSdU, P, eps);
+  // dSdU == NULL without P: only dS/drho is wanted (the thin-link result stays internal)
+  if (!P && dSdU && dSdU->kind != mk) throw gf_error(GF_EINVAL, "stout backward: dS/dU kind does not match the stack precision");
+  if (!P && !dSdU && !dsdrho) throw gf_error(GF_EINVAL, "stout backward: no output");
+  if (st->precision == GF_FP64) backward_impl<double>(ctx, st, dSdUbar, beta, dSdU, P, eps, dsdrho);
+  else if (st->precision == GF_PREC_DF) backward_df(ctx, st, dSdUbar, beta, dSdU, P, eps, dsdrho);
+  else backward_impl<float>(ctx, st, dSdUbar, beta, dSdU, P, eps, dsdrho);
 }
 
 }  // namespace gf

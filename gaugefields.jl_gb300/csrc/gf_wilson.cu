@@ -36,6 +36,10 @@ double plaquette_sum(gf_ctx* ctx, const gf_field* U, bool df) {
   } else if (U->kind == GF_LINK32) {
     Src32 src{(const float4*)U->ptr};
     k_plaquette<float><<<nb, 128, 0, ctx->stream>>>(src, ctx->geom, ctx->d_partials);
+  } else if (U->kind == GF_LINKDF) {
+    // top level of a double-float stack: fp64 arithmetic on hi + lo
+    LinkSrcDfn64 src{(const float4*)U->ptr};
+    k_plaquette<double><<<nb, 128, 0, ctx->stream>>>(src, ctx->geom, ctx->d_partials);
   } else {
     throw gf_error(GF_EINVAL, "plaquette: links must be LINK64 or LINK32");
   }

@@ -229,6 +229,66 @@ struct LinkFull<dfl> {
   }
 };
 
+// Double-float-native 18-real storage (the internal fields of double-float
+// stout stacks): each complex element is one float4 (re.hi, re.lo, im.hi,
+// im.lo), laid out like LINK64 / MAT64 (16 bytes per element, 144 per
+// link), so loads and stores need no fp64 <-> double-float conversion.
+struct LinkDfn {
+  typedef float4 elem;
+  static __device__ __forceinline__ mat3<dfl> load(const float4* __restrict__ p, int mu, int s, int V) {
+    mat3<dfl> m;
+    const float4* b = p + (size_t)mu * 9 * V + s;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      float4 v = __ldg(b + (size_t)k * V);
+      m.e[k / 3][k % 3] = mk(dfl(v.x, v.y), dfl(v.z, v.w));
+    }
+    return m;
+  }
+  // fp64 view of a double-float-native link (hi + lo in fp64; fp64 kernels)
+  static __device__ __forceinline__ mat3<double> load64(const float4* __restrict__ p, int mu, int s, int V) {
+    mat3<double> m;
+    const float4* b = p + (size_t)mu * 9 * V + s;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      float4 v = __ldg(b + (size_t)k * V);
+      m.e[k / 3][k % 3] = mk((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+    }
+    return m;
+  }
+  static __device__ __forceinline__ void store(float4* __restrict__ p, int mu, int s, int V, const mat3<dfl>& m) {
+    float4* b = p + (size_t)mu * 9 * V + s;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const cplx<dfl> v = m.e[k / 3][k % 3];
+      b[(size_t)k * V] = make_float4(v.re.hi, v.re.lo, v.im.hi, v.im.lo);
+    }
+  }
+};
+
+// double-float loads and stores from either storage: fp64 (double2,
+// converted) or double-float-native (float4)
+template <typename E>
+struct DfIO;
+template <>
+struct DfIO<double2> {
+  static __device__ __forceinline__ mat3<dfl> load(const double2* __restrict__ p, int mu, int s, int V) {
+    return LinkFull<dfl>::load(p, mu, s, V);
+  }
+  static __device__ __forceinline__ void store(double2* __restrict__ p, int mu, int s, int V, const mat3<dfl>& m) {
+    LinkFull<dfl>::store(p, mu, s, V, m);
+  }
+};
+template <>
+struct DfIO<float4> {
+  static __device__ __forceinline__ mat3<dfl> load(const float4* __restrict__ p, int mu, int s, int V) {
+    return LinkDfn::load(p, mu, s, V);
+  }
+  static __device__ __forceinline__ void store(float4* __restrict__ p, int mu, int s, int V, const mat3<dfl>& m) {
+    LinkDfn::store(p, mu, s, V, m);
+  }
+};
+
 // 12-real two-row fp32 link storage: 3 float4 per link
 struct Link12f {
   static __device__ __forceinline__ mat3<float> load(const float4* __restrict__ p, int mu, int s, int V) {
@@ -263,6 +323,13 @@ struct LinkSrc<R, false> {
   typedef typename LinkFull<R>::elem elem;
   const elem* __restrict__ p;
   __device__ __forceinline__ mat3<R> operator()(int mu, int s, int V) const { return LinkFull<R>::load(p, mu, s, V); }
+};
+// fp64 arithmetic on double-float-native storage (plaquette of a
+// double-float stack's top level)
+struct LinkSrcDfn64 {
+  typedef float4 elem;
+  const float4* __restrict__ p;
+  __device__ __forceinline__ mat3<double> operator()(int mu, int s, int V) const { return LinkDfn::load64(p, mu, s, V); }
 };
 template <>
 struct LinkSrc<float, true> {

@@ -12,6 +12,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
+#include <string.h>
 #include "dfloat.cuh"
 
 #define GF_HD __host__ __device__ __forceinline__
@@ -586,6 +587,104 @@ GF_HD mat3<dfl> df_matmul(const mat3<dfl>& a, const mat3<dfl>& b, const mat3<dfl
         dacc_add(im, x.im.hi, x.im.lo, y.re.hi, y.re.lo);
       }
       r.e[i][j] = mk(dacc_get(re), dacc_get(im));
+    }
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// Fixed-grid compensated product. The high parts of the terms of each output
+// are accumulated onto a grid: the accumulator starts at a constant
+// K = 1.5 * 2^k chosen from a norm bound so that every partial sum stays in
+// [2^k, 2^(k+1)), where fp32 spacing is the constant g = 2^(k-23). Then each
+// fused multiply-add a_h b_h + A rounds onto that grid, A - A_new is exact,
+// and a second fused multiply-add recovers the rounding residual
+// a_h b_h + (A - A_new) (about 24 bits, exact to 2^-48 relative). Residuals
+// and the cross terms a_h b_l + a_l b_h go to a plain fp32 correction. Six
+// fp32 operations per real term instead of the twelve of the TwoSum-based
+// accumulation above; the error is ~2^-44 of |op(A)| |op(B)| (+ |C|) per
+// entry, against ~2^-48 there. The bound: partial sums of entry (i,j) are at
+// most |row i of op(A)| |column j of op(B)| (Cauchy-Schwarz), so
+// M^2 = max_i |a_i|^2 max_j |b_j|^2 (+ the accumulator's entries), and k is
+// taken from M^2's exponent with a factor 2 of headroom.
+// ---------------------------------------------------------------------------
+GF_HD float df_grid_const(float m2) {
+#ifdef __CUDA_ARCH__
+  const int e2 = (int)(__float_as_uint(m2) >> 23);
+#else
+  unsigned int u;
+  memcpy(&u, &m2, 4);
+  const int e2 = (int)(u >> 23);
+#endif
+  // 2^(k-1) >= 2 M with M^2 < 2^(e2-126): k = ceil((e2 - 122) / 2)
+  const int k = (e2 - 121) >> 1;
+  const unsigned int bits = ((unsigned int)(k + 127) << 23) | 0x400000u;
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(bits);
+#else
+  float f;
+  memcpy(&f, &bits, 4);
+  return f;
+#endif
+}
+
+GF_HD void grid_term(float& A, float& L, float xh, float xl, float yh, float yl) {
+  const float An = fmaf(xh, yh, A);
+  const float t = A - An;  // exact: both on the grid of one binade
+  L += fmaf(xh, yh, t);    // the rounding residual of xh*yh onto the grid
+  L = fmaf(xh, yl, L);
+  L = fmaf(xl, yh, L);
+  A = An;
+}
+
+template <bool DA, bool DB, bool ACC, int ROWS = 3>
+GF_HD mat3<dfl> dfg_matmul(const mat3<dfl>& a, const mat3<dfl>& b, const mat3<dfl>* c) {
+  float ra = 0.f, cb = 0.f;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    float r = 0.f, q = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const cplx<dfl> x = DA ? conj(a.e[k][i]) : a.e[i][k];  // row i of op(a)
+      const cplx<dfl> y = DB ? conj(b.e[i][k]) : b.e[k][i];  // column i of op(b)
+      r = fmaf(x.re.hi, x.re.hi, fmaf(x.im.hi, x.im.hi, r));
+      q = fmaf(y.re.hi, y.re.hi, fmaf(y.im.hi, y.im.hi, q));
+    }
+    if (i < ROWS) ra = fmaxf(ra, r);
+    cb = fmaxf(cb, q);
+  }
+  float m2 = ra * cb;
+  if (ACC) {
+    float cm = 0.f;
+#pragma unroll
+    for (int i = 0; i < ROWS; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) cm = fmaxf(cm, fmaxf(fabsf(c->e[i][j].re.hi), fabsf(c->e[i][j].im.hi)));
+    m2 = 2.f * fmaf(cm, cm, m2);  // (x + y)^2 <= 2 (x^2 + y^2)
+  }
+  const float K = df_grid_const(m2);
+  mat3<dfl> r = zero3<dfl>();
+#pragma unroll
+  for (int i = 0; i < ROWS; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      float Ar = K, Ai = K, Lr = 0.f, Li = 0.f;
+      if (ACC) {
+        const cplx<dfl> v = c->e[i][j];
+        Ar = K + v.re.hi;
+        Lr = (v.re.hi - (Ar - K)) + v.re.lo;
+        Ai = K + v.im.hi;
+        Li = (v.im.hi - (Ai - K)) + v.im.lo;
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const cplx<dfl> x = DA ? conj(a.e[k][i]) : a.e[i][k];
+        const cplx<dfl> y = DB ? conj(b.e[j][k]) : b.e[k][j];
+        grid_term(Ar, Lr, x.re.hi, x.re.lo, y.re.hi, y.re.lo);
+        grid_term(Ar, Lr, -x.im.hi, -x.im.lo, y.im.hi, y.im.lo);
+        grid_term(Ai, Li, x.re.hi, x.re.lo, y.im.hi, y.im.lo);
+        grid_term(Ai, Li, x.im.hi, x.im.lo, y.re.hi, y.re.lo);
+      }
+      r.e[i][j] = mk(df_fast_two_sum(Ar - K, Lr), df_fast_two_sum(Ai - K, Li));
     }
   return r;
 }

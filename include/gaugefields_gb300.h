@@ -116,6 +116,9 @@ int gf_field_device_ptr(const gf_field* f, void** ptr);
 int gf_field_copy(gf_ctx* ctx, gf_field* dst, const gf_field* src);
 /* clear_U! */
 int gf_field_zero(gf_ctx* ctx, gf_field* f);
+/* add_U!(c, t, a) (src/4D/mpi_jacc/gaugefields_4D_MPILattice.jl:739-745):
+ * y += a x for fp64 fields of one kind (LINK64, MAT64 or MOM64). */
+int gf_field_axpy(gf_ctx* ctx, gf_field* y, double a, const gf_field* x);
 
 /* ---- host transfer in the reference layout ----------------------------- */
 /* Upload/download link fields (LINK64 or MAT64) and momenta (MOM64); the
@@ -218,6 +221,13 @@ int gf_stout_forward(gf_ctx* ctx, gf_stout* st, const gf_field* U, gf_field* Uou
  * backward_dSdUαUβρ_add! (stout_fast.jl:317-408): dS/dU on the thin links
  * from dS/dUbar (MAT64/MAT32 in the precision of the stack). */
 int gf_stout_backward(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, gf_field* dSdU);
+/* parameter_derivatives / get_parameter_derivatives (Abstractsmearing.jl:
+ * 416-436, 505; the rho part of backward_dSdUαUβρ_add!, stout_fast.jl:
+ * 371-386): forward on U, then the adjoint from dS/dUbar (MAT64, or MAT32
+ * for a GF_MIXED stack), writing dS/drho of every level to dSdrho[0..nlev-1]:
+ * dS/drho_l = 2 Re sum tr(Z_l S_l^dag), Z_l = dS/dC_l, C_l = rho_l S_l^dag. */
+int gf_stout_param_derivatives(gf_ctx* ctx, gf_stout* st, const gf_field* U, const gf_field* dSdUbar,
+                               double* dSdrho);
 /* Smeared Wilson-action MD force on the thin links, the stout-HMC P_update!
  * (test/HMCstout_test_nowing.jl:99-118): forward, dS/dUbar = beta/2 * staples
  * of Ubar, back-propagation, P += eps * (-(1/3) TA(U dS/dU)). */
@@ -252,8 +262,10 @@ int gf_flow_force(gf_ctx* ctx, const gf_field* U, gf_field* F, double factor);
  * GF_EINVAL. All calls share that array: calls whose kernels overlap on the
  * GPU race and must be serialised by the caller. The first call on a device
  * looks up the array's device address (cudaGetSymbolAddress) with that device
- * current; make it before any stream capture. gf_last_error(NULL) gives the
- * message of a failed call. */
+ * current; make it before any stream capture. That address is kept for the
+ * life of the process, so do not call this entry point again after
+ * cudaDeviceReset (or any teardown of the device's primary context).
+ * gf_last_error(NULL) gives the message of a failed call. */
 int gf_plaquette_noalloc(const void* links, const int L[4], double* out, void* stream);
 
 /* ---- instrumentation (no counterpart in the reference) ----------------- */

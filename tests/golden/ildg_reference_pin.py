@@ -14,9 +14,11 @@ reader uses and, for contrast, with every matrix transposed. The files are
 not copied. tests/test_ildg.py checks the record against the reference's
 number and, where the reference tree is present, reads the files again.
 
-    python tests/golden/ildg_reference_pin.py [reference-root]
+    GF_REFERENCE_ROOT=<reference checkout> python tests/golden/ildg_reference_pin.py
+    python tests/golden/ildg_reference_pin.py <reference checkout>
 
-The reference root defaults to GF_REFERENCE_ROOT, else /root/reference.
+The reference root is the argument, else the environment variable
+GF_REFERENCE_ROOT; there is no default location.
 """
 import hashlib
 import importlib.util
@@ -44,9 +46,10 @@ FIXTURES = {
 
 
 def reference_root(argv=()):
+    """The reference checkout to read, or None when none was given."""
     if argv:
         return argv[0]
-    return os.environ.get("GF_REFERENCE_ROOT", "/root/reference")
+    return os.environ.get("GF_REFERENCE_ROOT") or None
 
 
 def ildg_module():
@@ -103,6 +106,8 @@ def derive(root, name, spec, io=None):
 
 def main(argv):
     root = reference_root(argv)
+    if root is None:
+        sys.exit("give the reference checkout as the argument or in GF_REFERENCE_ROOT")
     out = {"reference_files": {}}
     for name, spec in FIXTURES.items():
         entry = dict(spec)

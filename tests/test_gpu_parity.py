@@ -344,31 +344,52 @@ def test_mixed_precision_stout_force_is_close(pkg):
     assert rel < 1e-5
 
 
-def test_mixed_precision_trajectory_delta_h(pkg):
-    results = {}
-    for prec in ("fp64", "mixed"):
-        U = pkg.gauge_configuration(L8, start="hot", seed=7)
-        P = pkg.gaussian_momenta(U, seed=1)
-        action = pkg.GaugeAction(U)
-        pkg.push_(action, 3.0, "plaquette")
-        net = pkg.stout_smearing(U, rho=0.1)
-        pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
-        drv = pkg.md_driver(U, action, steps=20, smearing=net, precision=prec)
-        results[prec] = pkg.md_trajectory_(U, P, drv)
-    # Same start and momenta: the fp64 Hamiltonian at the start is identical;
-    # the fp32 force changes Delta H by a random walk of its rounding errors.
-    # On this unthermalised hot start (Delta H ~ 130) the bound is relative.
-    h0 = results["fp64"].initial_hamiltonian
-    assert abs(results["mixed"].initial_hamiltonian - h0) <= 1e-12 * abs(h0)
-    d64 = results["fp64"].delta_hamiltonian
-    assert abs(results["mixed"].delta_hamiltonian - d64) < 1e-4 * max(1.0, abs(d64))
+@pytest.fixture(scope="module")
+def thermalised8(pkg):
+    """An 8^4 configuration with Delta H of order one at beta = 6.0 on two
+    stout levels: a cold start, then 10 plain fp64 trajectories (tau = 1, 20
+    QPQ steps) kept unconditionally."""
+    U = pkg.gauge_configuration(L8, start="cold")
+    P = pkg.gauge_momenta(U)
+    drv = _smeared(pkg, U, 6.0, "fp64", steps=20, levels=2)
+    for t in range(10):
+        pkg.gaussian_momenta_(P, seed=5, sweep=t)
+        pkg.md_trajectory_(U, P, drv)
+    return U.to_host()
 
 
-def _smeared(pkg, U, beta, prec, steps=10):
+@pytest.mark.parametrize("prec,tol", [("mixed", 1e-4), ("dfloat", 1e-8)])
+def test_precision_form_trajectory_delta_h(pkg, thermalised8, prec, tol):
+    """Three 2-level stout trajectories (beta = 6.0, tau = 1, 20 QPQ steps) from
+    the same thermalised 8^4 configuration with the same momenta in the plain
+    fp64 form and the fast form: the fp64 Hamiltonian at the start is
+    identical, and |Delta H_form - Delta H_fp64| <= tol absolute (the
+    bound of the precision target, 1e-4; 1e-8 for double-float). The fp32
+    force of the mixed form moves Delta H by a random walk of its rounding
+    errors that grows with the square root of the volume: it stays inside
+    1e-4 at 8^4 but not at 32^4 (the benchmark's Delta H study), which is why
+    the double-float form is the benchmark's headline."""
+    for traj in range(3):
+        res = {}
+        for p in ("fp64", prec):
+            U = pkg.gauge_configuration(L8, start="cold")
+            U.from_host(thermalised8)
+            P = pkg.gaussian_momenta(U, seed=11, sweep=traj)
+            res[p] = pkg.md_trajectory_(U, P, _smeared(pkg, U, 6.0, p, steps=20, levels=2))
+        h0 = res["fp64"].initial_hamiltonian
+        assert abs(res[prec].initial_hamiltonian - h0) <= 1e-12 * abs(h0)
+        d64 = res["fp64"].delta_hamiltonian
+        assert abs(d64) < 5.0  # Delta H of order one
+        assert abs(res[prec].delta_hamiltonian - d64) <= tol, (traj, res[prec].delta_hamiltonian, d64)
+
+
+def _smeared(pkg, U, beta, prec, steps=10, levels=2):
+    """An MD driver for the Wilson action on `levels` stout levels, rho = 0.1."""
     action = pkg.GaugeAction(U)
     pkg.push_(action, beta / 2, "plaquette")
     net = pkg.stout_smearing(U, rho=0.1)
-    pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
+    for _ in range(levels - 1):
+        pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
     return pkg.md_driver(U, action, steps=steps, smearing=net, precision=prec)
 
 

@@ -181,6 +181,8 @@ def test_reference_ildg_files_pin_the_payload_order(io):
             pinned += 1
     assert pinned == 1
     root = pin.reference_root()
+    if root is None:
+        pytest.skip("GF_REFERENCE_ROOT not set; checked the record only")
     present = [n for n in record if os.path.exists(os.path.join(root, n))]
     if not present:
         pytest.skip("reference test files not present; checked the record only")

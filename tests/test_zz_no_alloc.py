@@ -62,3 +62,30 @@ def test_noalloc_plaquette_rejects_oversized_lattices(pkg):
     assert _call(lib, U, L, 0x1000, 0) == _lib.GF_EINVAL
     assert b"at most 16777216" in lib.gf_last_error(None)
     assert _call(lib, U, (3, 4, 4, 4), 0x1000, 0) == _lib.GF_EINVAL
+    # extents whose product overflows 64 bits are rejected, not wrapped
+    big = 1 << 16
+    assert _call(lib, U, (big, big, big, big), 0x1000, 0) == _lib.GF_EINVAL
+    assert _call(lib, U, (2, 2, 2, (1 << 30)), 0x1000, 0) == _lib.GF_EINVAL
+
+
+def test_noalloc_plaquette_leaves_device_memory_untouched(pkg):
+    """After the first call (which looks up the array's address), further
+    calls change neither the device's free memory nor PyTorch's allocator."""
+    import torch
+    from gaugefields_gb300 import _lib
+    lib = _lib.load()
+    L = (8, 8, 8, 8)
+    U = pkg.gauge_configuration(L, start="hot", seed=3)
+    U.ctx.sync()
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    assert _call(lib, U, L, out.data_ptr(), stream) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    alloc0, reserved0 = torch.cuda.memory_allocated(), torch.cuda.memory_reserved()
+    for _ in range(20):
+        assert _call(lib, U, L, out.data_ptr(), stream) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert torch.cuda.memory_allocated() == alloc0 and torch.cuda.memory_reserved() == reserved0
