@@ -304,7 +304,7 @@ def e2e_hmc(pkg, torch, L, steps, warmup, rank, form=HEADLINE_FORM):
             "d2h_bytes_per_step": 36 * V * 16 + 3 * 8, "ms_per_step": 1e3 * sec / steps}
 
 
-def dh_study(pkg, torch, L, ntherm, ntraj, forms=("fp64", "mixed"), md_steps=None, start="cold"):
+def dh_study(pkg, torch, L, ntherm, ntraj, forms=("fp64", "mixed"), md_steps=None, start="cold", progress=False):
     """|Delta H_form - Delta H_fp64| over `ntraj` trajectories, each from the
     same thermalised configuration with the same fresh momenta in every form;
     the Metropolis decisions use the same uniform. Thermalisation: a cold
@@ -345,16 +345,23 @@ def dh_study(pkg, torch, L, ntherm, ntraj, forms=("fp64", "mixed"), md_steps=Non
             row["plaq_diff_" + f] = abs(r[f][1] - r["fp64"][1])
             row["same_decision_" + f] = bool(acc64 == (u < np.exp(-r[f][0])))
         rows.append(row)
+        if progress:
+            print(json.dumps(dict(row, trajectory=i)), file=sys.stderr, flush=True)
     out = {"lattice": [L] * 4, "md_steps": md_steps or NSTEPS, "trajectories": len(rows),
            "start": "%s start + %d mixed trajectories kept unconditionally (plaquette %.6f)" % (start, ntherm, plaq0),
            "therm_seconds": t_therm, "dH_fp64_median_abs": float(np.median([abs(x["dH_fp64"]) for x in rows])),
            "seconds_per_trajectory": {f: secs[f] / len(rows) for f in forms}}
+    pacc = lambda dh: min(1.0, float(np.exp(-dh)))  # noqa: E731 (Metropolis acceptance probability)
+    out["fp64_acceptance_mean"] = float(np.mean([pacc(x["dH_fp64"]) for x in rows]))
     for f in forms[1:]:
         d = [x["abs_diff_" + f] for x in rows]
         out[f] = {"abs_dH_diff_median": float(np.median(d)), "abs_dH_diff_max": max(d),
                   "within_1e-4": sum(v <= 1e-4 for v in d),
                   "same_decision": sum(x["same_decision_" + f] for x in rows),
-                  "plaq_diff_max": max(x["plaq_diff_" + f] for x in rows)}
+                  "plaq_diff_max": max(x["plaq_diff_" + f] for x in rows),
+                  "acceptance_mean": float(np.mean([pacc(x["dH_" + f]) for x in rows])),
+                  # expected number of decisions the Delta H difference flips
+                  "sum_abs_acceptance_diff": float(sum(abs(pacc(x["dH_" + f]) - pacc(x["dH_fp64"])) for x in rows))}
     return out, rows
 
 
@@ -451,8 +458,8 @@ def run_precision_mode(args):
     import __graft_entry__ as entry
     pkg = entry.build()
     L = args.lattice
-    forms = ("fp64", "mixed") + (() if args.no_dfloat else ("dfloat",))
-    out, rows = dh_study(pkg, torch, L, args.therm, args.steps, forms, args.md_steps, start="hot")
+    forms = ("fp64",) + (() if args.no_mixed else ("mixed",)) + (() if args.no_dfloat else ("dfloat",))
+    out, rows = dh_study(pkg, torch, L, args.therm, args.steps, forms, args.md_steps, start="hot", progress=True)
     out = dict({"mode": "precision", "workload": workload_name(L), "therm": args.therm}, **out)
     out["rows"] = rows
     print(json.dumps(out))
@@ -610,13 +617,18 @@ def run_scale_mode(args):
 
 def run_kernel_mode(args):
     """Small single-family cases for profiler captures: `force` repeats the
-    stout force of the workload (update_momenta_), `link` the link update
-    (update_gaugefields_), both in the form `--precision` names."""
+    stout force of the workload (update_momenta_; `--levels 0`: the Wilson
+    force on thin links), `link` the link update (update_gaugefields_), both
+    in the form `--precision` names, and `plaquette` the plaquette sum."""
     import torch
     import __graft_entry__ as entry
     pkg = entry.build()
     L = args.lattice
     U, P, drv = make_setup(pkg, L, args.precision, SEED)
+    if args.levels == 0:
+        action = pkg.GaugeAction(U)
+        pkg.push_(action, BETA / 2, "plaquette")
+        drv = pkg.md_driver(U, action, steps=NSTEPS, trajectory_length=TAU, precision=args.precision)
     pkg.gaussian_momenta_(P, seed=SEED)
     calls = []
     for k in range(args.warmup + args.steps):
@@ -624,11 +636,14 @@ def run_kernel_mode(args):
         t0 = time.perf_counter()
         if args.mode == "force":
             pkg.update_momenta_(P, U, 0.01, drv)
-        else:
+        elif args.mode == "link":
             pkg.update_gaugefields_(U, P, 0.01, drv)
+        else:
+            pkg.calculate_Plaquette(U)
         U.ctx.sync()
         calls.append(time.perf_counter() - t0)
     print(json.dumps({"mode": args.mode, "precision": args.precision, "lattice": [L] * 4,
+                      "stout_levels": len(RHO) if args.levels is None else args.levels,
                       "ms_per_call": 1e3 * min(calls[args.warmup:])}))
     return 0
 
@@ -653,7 +668,9 @@ def main():
                     help="form of the force/link modes")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--therm", type=int, default=10, help="thermalisation trajectories before the Delta H check")
-    ap.add_argument("--mode", default="hmc", choices=["hmc", "force", "link", "precision", "wilson", "scale"],
+    ap.add_argument("--levels", type=int, default=None, help="force mode: 0 = Wilson force without smearing")
+    ap.add_argument("--mode", default="hmc", choices=["hmc", "force", "link", "plaquette", "precision", "wilson",
+                                                      "scale"],
                     help="hmc: the benchmark; force/link: one kernel family, for profiler captures; "
                          "precision: mixed vs fp64 Delta H study from one thermalised configuration")
     args = ap.parse_args()

@@ -245,26 +245,25 @@ struct DfOp {
   unsigned char a_src, a_dir, a_site, a_dag, b_src, b_dir, b_site, b_dag, out, accumulate;
 };
 
-// slot `slot` of this thread: 36 floats, element-major so that a warp's
-// accesses fall in consecutive banks (blocks of 128 threads)
+// slot `slot` of this thread: 9 float4 (one per complex element),
+// element-major, so a warp's 128-bit accesses cover consecutive banks
+// (blocks of 128 threads; 36 floats per thread and slot)
 __device__ __forceinline__ mat3<dfl> slot_load(const float* sm, int slot, int tid) {
   mat3<dfl> m;
+  const float4* q = reinterpret_cast<const float4*>(sm) + slot * 9 * 128 + tid;
 #pragma unroll
   for (int e = 0; e < 9; ++e) {
-    const float* q = sm + (slot * 36 + 4 * e) * 128 + tid;
-    m.e[e / 3][e % 3] = mk(dfl(q[0], q[128]), dfl(q[256], q[384]));
+    const float4 v = q[e * 128];
+    m.e[e / 3][e % 3] = mk(dfl(v.x, v.y), dfl(v.z, v.w));
   }
   return m;
 }
 __device__ __forceinline__ void slot_store(float* sm, int slot, int tid, const mat3<dfl>& m) {
+  float4* q = reinterpret_cast<float4*>(sm) + slot * 9 * 128 + tid;
 #pragma unroll
   for (int e = 0; e < 9; ++e) {
-    float* q = sm + (slot * 36 + 4 * e) * 128 + tid;
     const cplx<dfl> v = m.e[e / 3][e % 3];
-    q[0] = v.re.hi;
-    q[128] = v.re.lo;
-    q[256] = v.im.hi;
-    q[384] = v.im.lo;
+    q[e * 128] = make_float4(v.re.hi, v.re.lo, v.im.hi, v.im.lo);
   }
 }
 
@@ -299,6 +298,9 @@ __device__ __forceinline__ void df_exec(const DfOp op, float* sm, int tid, const
                                         int d1, const DfSites& st) {
   const mat3<dfl> A = df_operand(op.a_src, op.a_dir, op.a_site, op.a_dag, sm, tid, F, V, d0, d1, st);
   const mat3<dfl> B = df_operand(op.b_src, op.b_dir, op.b_site, op.b_dag, sm, tid, F, V, d0, d1, st);
+  // one inlined product, always accumulating (into zero when the op does not
+  // accumulate): a second, non-accumulating copy in the loop body measured
+  // 3% slower per trajectory (larger body)
   const mat3<dfl> C = op.accumulate ? slot_load(sm, op.out, tid) : zero3<dfl>();
 #if GF_DF_GRID
   slot_store(sm, op.out, tid, dfg_matmul<false, false, true>(A, B, &C));
@@ -331,7 +333,7 @@ template <bool FORCE, typename EOUT>
 __global__ void __launch_bounds__(128, GF_DF_GATHER_MINB)
     k_bwd_gather_df(const float4* __restrict__ U, const float4* __restrict__ Z, const float4* __restrict__ Dp,
                     EOUT* __restrict__ Dout, double* __restrict__ P, Geom g, dfl rho, double coef) {
-  __shared__ float sm[2 * 36 * 128];
+  __shared__ __align__(16) float sm[2 * 36 * 128];
   const int tid = threadIdx.x;
   int s, nu;
   link_of_thread(s, nu);
@@ -367,6 +369,17 @@ __global__ void __launch_bounds__(128, GF_DF_GATHER_MINB)
   }
 }
 
+// Fixed-grid double-float products with compile-time operand forms (the
+// register-resident kernels below)
+template <bool DA, bool DB>
+__device__ __forceinline__ mat3<dfl> dfr_mul(const mat3<dfl>& a, const mat3<dfl>& b) {
+  return dfg_matmul<DA, DB, false>(a, b, nullptr);
+}
+template <bool DA, bool DB>
+__device__ __forceinline__ void dfr_mac(mat3<dfl>& acc, const mat3<dfl>& a, const mat3<dfl>& b) {
+  acc = dfg_matmul<DA, DB, true>(a, b, &acc);
+}
+
 // The stout forward: F0 = U, d0 = mu, d1 = nu; sites x, x+mu, x+nu,
 // x+mu-nu, x-nu; slot 0 = t, slot 1 = acc. Ops 0-3 (per nu) build S_mu in
 // dS/dU order as add_staple_pair does; op 4 forms U S; op 5 e^Q U.
@@ -388,7 +401,7 @@ template <typename EIN>
 __global__ void __launch_bounds__(128, GF_DF_FWD_MINB)
     k_stout_fwd_df(const EIN* __restrict__ U, float4* __restrict__ Uout, float4* __restrict__ Cout, Geom g,
                    dfl rho) {
-  __shared__ float sm[2 * 36 * 128];
+  __shared__ __align__(16) float sm[2 * 36 * 128];
   const int tid = threadIdx.x;
   int s, mu;
   link_of_thread(s, mu);
@@ -419,6 +432,112 @@ __global__ void __launch_bounds__(128, GF_DF_FWD_MINB)
   }
   if (live) LinkDfn::store(Uout, mu, s, V, slot_load(sm, 1, tid));
 }
+
+// S_mu(x) (the six staples in dS/dU order, as staple_sum) with fixed-grid
+// double-float products, from either storage
+template <typename E>
+__device__ __forceinline__ mat3<dfl> staple_sum_dfr(const E* __restrict__ U, int mu, const Geom& g, const Site& st,
+                                                    int s) {
+  const int V = g.vol;
+  const int xpm = nbr_rt(g, st, mu, +1);
+  mat3<dfl> S = zero3<dfl>();
+#pragma unroll 1
+  for (int k = 1; k < 4; ++k) {
+    const int nu = (mu + k) & 3;
+    const int xpn = nbr_rt(g, st, nu, +1);
+    const int xmn = nbr_rt(g, st, nu, -1);
+    const int xpm_mn = nbr2_rt(g, st, mu, +1, nu, -1);
+    // up: U_nu(x+mu) U_mu(x+nu)^dag U_nu(x)^dag
+    mat3<dfl> t = dfr_mul<false, true>(DfIO<E>::load(U, nu, xpm, V), DfIO<E>::load(U, mu, xpn, V));
+    dfr_mac<false, true>(S, t, DfIO<E>::load(U, nu, s, V));
+    // down: U_nu(x+mu-nu)^dag U_mu(x-nu)^dag U_nu(x-nu)
+    t = dfr_mul<true, true>(DfIO<E>::load(U, nu, xpm_mn, V), DfIO<E>::load(U, mu, xmn, V));
+    dfr_mac<false, false>(S, t, DfIO<E>::load(U, nu, xmn, V));
+  }
+  return S;
+}
+
+// The local adjoint with products in registers (the register form of
+// k_bwd_local_df, same order of operations). C and Dbar wait in two
+// per-thread shared-memory slots between their uses, which keeps the kernel
+// within the register file.
+#ifndef GF_DF_LOCAL_REG_MINB
+#define GF_DF_LOCAL_REG_MINB 2
+#endif
+template <bool TOP>
+__global__ void __launch_bounds__(128, GF_DF_LOCAL_REG_MINB)
+    k_bwd_local_dfr(const float4* __restrict__ U, const float4* __restrict__ F1, const float4* __restrict__ Cst,
+                    float4* __restrict__ Zout, float4* __restrict__ Dpout, Geom g, dfl rho, dfl halfbeta) {
+  __shared__ __align__(16) float sm[2 * 36 * 128];
+  const int tid = threadIdx.x;
+  int s, mu;
+  link_of_thread(s, mu);
+  if (s >= g.vol) return;  // the slots are per thread: no block-wide synchronisation
+  const int V = g.vol;
+  const Site st = site_of(g, s);
+  {
+    const mat3<dfl> C = Cst ? LinkDfn::load(Cst, mu, s, V) : scale(rho, dag(staple_sum_dfr(U, mu, g, st, s)));
+    slot_store(sm, 0, tid, C);
+  }
+  {
+    // top level: Dbar = beta/2 S(Ubar_top)
+    const mat3<dfl> db = TOP ? scale(halfbeta, staple_sum_dfr(F1, mu, g, st, s)) : LinkDfn::load(F1, mu, s, V);
+    slot_store(sm, 1, tid, db);
+  }
+  const mat3<dfl> u = LinkDfn::load(U, mu, s, V);
+  // Qh = -i TA(C U^dag)
+  const mat3<dfl> qh = times_i(dfl(-1), ta_proj(dfr_mul<false, true>(slot_load(sm, 0, tid), u)));
+  dfl c0, c1;
+  herm_invariants(qh, c0, c1);
+  ch_coef<dfl> cc;
+  ch_coefficients<dfl, true>(c0, c1, cc);
+  const mat3<dfl> qh2 = herm_square(qh);
+  mat3<dfl> Y;
+  {
+    const mat3<dfl> lam = dfr_mul<false, false>(u, slot_load(sm, 1, tid));  // Lambda = U Dbar
+    const cplx<dfl> trL = trace(lam), trLQ = tr_nn(lam, qh), trLQ2 = tr_nn(lam, qh2);
+    const cplx<dfl> trB1 = cc.b1[0] * trL + cc.b1[1] * trLQ + cc.b1[2] * trLQ2;
+    const cplx<dfl> trB2 = cc.b2[0] * trL + cc.b2[1] * trLQ + cc.b2[2] * trLQ2;
+    // Gamma = trB1 Qh + trB2 Qh^2 + f1 Lambda + f2 (Qh Lambda + Lambda Qh)
+    mat3<dfl> gam = dfr_mul<false, false>(qh, lam);
+    dfr_mac<false, false>(gam, lam, qh);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        cplx<dfl> v = cc.f[2] * gam.e[i][j];
+        fma_(v, cc.f[1], lam.e[i][j]);
+        fma_(v, trB1, qh.e[i][j]);
+        fma_(v, trB2, qh2.e[i][j]);
+        gam.e[i][j] = v;
+      }
+    Y = ta_proj(times_i(dfl(-1), gam));  // Y = TA(dS/dQ), dS/dQ = -i Gamma
+  }
+  LinkDfn::store(Zout, mu, s, V, dfr_mul<true, false>(u, Y));  // Z = U^dag Y
+  // exp(Q) = f0 + f1 Qh + f2 Qh^2;  Dp = Dbar e^Q + (Y C)^dag
+  mat3<dfl> E;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      cplx<dfl> w = cc.f[1] * qh.e[i][j];
+      fma_(w, cc.f[2], qh2.e[i][j]);
+      if (i == j) w = w + cc.f[0];
+      E.e[i][j] = w;
+    }
+  mat3<dfl> dp = dfr_mul<false, false>(slot_load(sm, 1, tid), E);
+  dfr_mac<true, true>(dp, slot_load(sm, 0, tid), Y);
+  LinkDfn::store(Dpout, mu, s, V, dp);
+}
+
+// the local adjoint form: 1 registers (k_bwd_local_dfr), 0 the table loop.
+// At 32^4 the register form takes 7.7 ms per launch, the table loop 8.0 ms.
+// For the forward and the gather the table loop is faster (4.1 against 4.5 ms,
+// 5.8 against 8.8 ms): their register forms inline 14 and 10 products per
+// loop body and run two blocks per SM (255 registers) against three.
+#ifndef GF_DF_LOCAL_REG
+#define GF_DF_LOCAL_REG 1
+#endif
 
 // The local adjoint: F0 = U, F1 = Dbar (or the top level's smeared links),
 // F2 = the stored C; d0 = mu, d1 = nu; sites x, x+mu, x+nu, x+mu-nu, x-nu.
@@ -681,12 +800,18 @@ static void backward_df(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, doub
     const float4* u = (const float4*)st->lev_in[l]->ptr;
     {
       ProfScope prof(ctx, GF_K_BWD_LOCAL_DF);
-      const size_t smem = (size_t)GF_LOCAL_SLOTS * 36 * 128 * sizeof(float);
-      auto kern = top ? k_bwd_local_df<true> : k_bwd_local_df<false>;
-      GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      kern<<<grid, 128, smem, ctx->stream>>>(u, top ? (const float4*)st->lev_in[l + 1]->ptr : din, Cst,
-                                             (float4*)st->Z->ptr, (float4*)st->Dp->ptr, ctx->geom, (dfl)st->rho[l],
-                                             (dfl)(0.5 * beta));
+      const float4* f1 = top ? (const float4*)st->lev_in[l + 1]->ptr : din;
+      if (GF_DF_LOCAL_REG) {
+        auto kern = top ? k_bwd_local_dfr<true> : k_bwd_local_dfr<false>;
+        kern<<<grid, 128, 0, ctx->stream>>>(u, f1, Cst, (float4*)st->Z->ptr, (float4*)st->Dp->ptr, ctx->geom,
+                                            (dfl)st->rho[l], (dfl)(0.5 * beta));
+      } else {
+        const size_t smem = (size_t)GF_LOCAL_SLOTS * 36 * 128 * sizeof(float);
+        auto kern = top ? k_bwd_local_df<true> : k_bwd_local_df<false>;
+        GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<grid, 128, smem, ctx->stream>>>(u, f1, Cst, (float4*)st->Z->ptr, (float4*)st->Dp->ptr, ctx->geom,
+                                               (dfl)st->rho[l], (dfl)(0.5 * beta));
+      }
       GF_CHECK_LAUNCH();
     }
     if (dsdrho) dsdrho[l] = level_dsdrho(ctx, st, l);

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
+#include <type_traits>
 #include "dfloat.cuh"
 
 #define GF_HD __host__ __device__ __forceinline__
@@ -389,33 +390,58 @@ __device__ __forceinline__ float inv_fact<float>(int n) { return c_inv_fact_f[n]
 template <>
 __device__ __forceinline__ dfl inv_fact<dfl>(int n) { return dfl(c_inv_fact_df[2 * n], c_inv_fact_df[2 * n + 1]); }
 
+// Accumulation and convergence helpers of the series: fp32/fp64 use the
+// plain operators; double-float accumulates with the sloppy double-word sum
+// (the terms shrink geometrically, so no cancellation) and measures the
+// term sizes on the fp32 high parts.
+template <typename R>
+struct ch_ops {
+  typedef R mag_t;
+  static __device__ __forceinline__ R sum(R x, R y) { return x + y; }
+  static __device__ __forceinline__ void add(R& x, R y) { x += y; }
+  static __device__ __forceinline__ void sub(R& x, R y) { x -= y; }
+  static __device__ __forceinline__ mag_t mag(R x) { return fabs(x); }
+  static __device__ __forceinline__ mag_t eps() { return ch_eps<R>(); }
+};
+template <>
+struct ch_ops<dfl> {
+  typedef float mag_t;
+  static __device__ __forceinline__ dfl sum(dfl x, dfl y) { return df_add_fast(x, y); }
+  static __device__ __forceinline__ void add(dfl& x, dfl y) { x = df_add_fast(x, y); }
+  static __device__ __forceinline__ void sub(dfl& x, dfl y) { x = df_add_fast(x, -y); }
+  static __device__ __forceinline__ float mag(dfl x) { return fabsf(x.hi); }
+  static __device__ __forceinline__ float eps() { return 2.0e-16f; }
+};
+
 // One term of the series: advance the power coefficients from Q^{n-1} to
 // Q^n and add i^n/n! times them; the phase i^n is the compile-time PH
 // (0: 1, 1: i, 2: -1, 3: -i), so each term costs adds only.
 template <typename R, bool DERIV, int PH>
 struct ch_state {
-  static __device__ __forceinline__ R step(int n, R c0, R c1, R& a, R& b, R& c, R& a0, R& b0, R& c0d, R& a1, R& b1,
-                                           R& c1d, R* fr, R* fi, R* d1r, R* d1i, R* d2r, R* d2i) {
-    R na = c0 * c, nb = a + c1 * c, nc = b;
+  typedef ch_ops<R> O;
+  static __device__ __forceinline__ typename O::mag_t step(int n, R c0, R c1, R& a, R& b, R& c, R& a0, R& b0, R& c0d,
+                                                          R& a1, R& b1, R& c1d, R* fr, R* fi, R* d1r, R* d1i,
+                                                          R* d2r, R* d2i) {
+    R na = c0 * c, nb = O::sum(a, c1 * c), nc = b;
     R na0 = 0, nb0 = 0, nc0 = 0, na1 = 0, nb1 = 0, nc1 = 0;
     if (DERIV) {
-      na0 = c + c0 * c0d;
-      nb0 = a0 + c1 * c0d;
+      na0 = O::sum(c, c0 * c0d);
+      nb0 = O::sum(a0, c1 * c0d);
       nc0 = b0;
       na1 = c0 * c1d;
-      nb1 = a1 + c + c1 * c1d;
+      nb1 = O::sum(O::sum(a1, c), c1 * c1d);
       nc1 = b1;
     }
     a = na; b = nb; c = nc;
     const R fact = inv_fact<R>(n);
     R t[3] = {a * fact, b * fact, c * fact};
-    R mag = fabs(t[0]) + fabs(t[1]) + fabs(t[2]);
+    typename O::mag_t mag = O::mag(t[0]) + O::mag(t[1]) + O::mag(t[2]);
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      if (PH == 0) fr[j] += t[j];
-      if (PH == 1) fi[j] += t[j];
-      if (PH == 2) fr[j] -= t[j];
-      if (PH == 3) fi[j] -= t[j];
+      if (PH == 0) O::add(fr[j], t[j]);
+      if (PH == 1) O::add(fi[j], t[j]);
+      if (PH == 2) O::sub(fr[j], t[j]);
+      if (PH == 3) O::sub(fi[j], t[j]);
     }
     if (DERIV) {
       a0 = na0; b0 = nb0; c0d = nc0;
@@ -424,19 +450,74 @@ struct ch_state {
       R u1[3] = {a1 * fact, b1 * fact, c1d * fact};
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        if (PH == 0) { d2r[j] += u0[j]; d1r[j] += u1[j]; }
-        if (PH == 1) { d2i[j] += u0[j]; d1i[j] += u1[j]; }
-        if (PH == 2) { d2r[j] -= u0[j]; d1r[j] -= u1[j]; }
-        if (PH == 3) { d2i[j] -= u0[j]; d1i[j] -= u1[j]; }
+        if (PH == 0) { O::add(d2r[j], u0[j]); O::add(d1r[j], u1[j]); }
+        if (PH == 1) { O::add(d2i[j], u0[j]); O::add(d1i[j], u1[j]); }
+        if (PH == 2) { O::sub(d2r[j], u0[j]); O::sub(d1r[j], u1[j]); }
+        if (PH == 3) { O::sub(d2i[j], u0[j]); O::sub(d1i[j], u1[j]); }
       }
-      mag += fabs(u0[0]) + fabs(u0[1]) + fabs(u0[2]) + fabs(u1[0]) + fabs(u1[1]) + fabs(u1[2]);
+      mag += O::mag(u0[0]) + O::mag(u0[1]) + O::mag(u0[2]) + O::mag(u1[0]) + O::mag(u1[1]) + O::mag(u1[2]);
     }
     return mag;
   }
 };
 
+// Double-float form: the terms are summed in double-float while the last
+// term of a group of four is at least 1e-8; the rest of the series, terms
+// below 1e-8, runs in fp32 (its rounding, ~1e-7 of the tail, is below 1e-15
+// absolute) and is added to the double-float sums at the end. For the
+// |Q| ~ 0.1-0.3 of stout layers and link updates this halves the number of
+// double-float terms.
+template <bool DERIV>
+__device__ __forceinline__ void ch_coefficients_df(dfl c0, dfl c1, ch_coef<dfl>& out) {
+  dfl a = dfl(1.f), b = dfl(0.f), c = dfl(0.f);
+  dfl a0 = 0, b0 = 0, c0d = 0, a1 = 0, b1 = 0, c1d = 0;
+  dfl fr[3] = {dfl(1.f), dfl(0.f), dfl(0.f)}, fi[3] = {0, 0, 0};
+  dfl d1r[3] = {0, 0, 0}, d1i[3] = {0, 0, 0}, d2r[3] = {0, 0, 0}, d2i[3] = {0, 0, 0};
+  int n = 1;
+  for (; n + 3 < GF_CH_TERMS; n += 4) {
+    ch_state<dfl, DERIV, 1>::step(n, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
+    ch_state<dfl, DERIV, 2>::step(n + 1, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
+    ch_state<dfl, DERIV, 3>::step(n + 2, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
+    const float mag =
+        ch_state<dfl, DERIV, 0>::step(n + 3, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
+    if (mag < 1.0e-8f) {
+      n += 4;
+      break;
+    }
+  }
+  // fp32 tail from term n (n = 1 mod 4, so the phases continue in order)
+  float fa = a.hi + a.lo, fb = b.hi + b.lo, fc = c.hi + c.lo;
+  float fa0 = a0.hi + a0.lo, fb0 = b0.hi + b0.lo, fc0 = c0d.hi + c0d.lo;
+  float fa1 = a1.hi + a1.lo, fb1 = b1.hi + b1.lo, fc1 = c1d.hi + c1d.lo;
+  const float g0 = c0.hi + c0.lo, g1 = c1.hi + c1.lo;
+  float tr[3] = {0.f, 0.f, 0.f}, ti[3] = {0.f, 0.f, 0.f};
+  float e1r[3] = {0.f, 0.f, 0.f}, e1i[3] = {0.f, 0.f, 0.f}, e2r[3] = {0.f, 0.f, 0.f}, e2i[3] = {0.f, 0.f, 0.f};
+  for (; n + 3 < GF_CH_TERMS; n += 4) {
+    ch_state<float, DERIV, 1>::step(n, g0, g1, fa, fb, fc, fa0, fb0, fc0, fa1, fb1, fc1, tr, ti, e1r, e1i, e2r, e2i);
+    ch_state<float, DERIV, 2>::step(n + 1, g0, g1, fa, fb, fc, fa0, fb0, fc0, fa1, fb1, fc1, tr, ti, e1r, e1i, e2r,
+                                    e2i);
+    ch_state<float, DERIV, 3>::step(n + 2, g0, g1, fa, fb, fc, fa0, fb0, fc0, fa1, fb1, fc1, tr, ti, e1r, e1i, e2r,
+                                    e2i);
+    const float mag = ch_state<float, DERIV, 0>::step(n + 3, g0, g1, fa, fb, fc, fa0, fb0, fc0, fa1, fb1, fc1, tr, ti,
+                                                      e1r, e1i, e2r, e2i);
+    if (mag < 2.0e-16f) break;
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    out.f[j] = mk(df_add_fast(fr[j], dfl(tr[j])), df_add_fast(fi[j], dfl(ti[j])));
+    if (DERIV) {
+      out.b1[j] = mk(df_add_fast(d1r[j], dfl(e1r[j])), df_add_fast(d1i[j], dfl(e1i[j])));
+      out.b2[j] = mk(df_add_fast(d2r[j], dfl(e2r[j])), df_add_fast(d2i[j], dfl(e2i[j])));
+    }
+  }
+}
+
 template <typename R, bool DERIV>
 __device__ __forceinline__ void ch_coefficients(R c0, R c1, ch_coef<R>& out) {
+  if constexpr (std::is_same<R, dfl>::value) {
+    ch_coefficients_df<DERIV>(c0, c1, out);
+    return;
+  }
   // power coefficients of Q^n and their partial derivatives
   R a = R(1), b = R(0), c = R(0);
   R a0 = 0, b0 = 0, c0d = 0;  // d/dc0
@@ -448,8 +529,9 @@ __device__ __forceinline__ void ch_coefficients(R c0, R c1, ch_coef<R>& out) {
     ch_state<R, DERIV, 1>::step(n, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
     ch_state<R, DERIV, 2>::step(n + 1, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
     ch_state<R, DERIV, 3>::step(n + 2, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
-    R mag = ch_state<R, DERIV, 0>::step(n + 3, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
-    if (mag < ch_eps<R>()) break;
+    const auto mag =
+        ch_state<R, DERIV, 0>::step(n + 3, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
+    if (mag < ch_ops<R>::eps()) break;
   }
 #pragma unroll
   for (int j = 0; j < 3; ++j) {

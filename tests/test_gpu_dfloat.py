@@ -48,13 +48,17 @@ def test_dfloat_stout_force_matches_oracle(pkg, oracle, L):
 
 
 def test_dfloat_stout_force_recompute_matches_store(pkg):
+    """Recomputing C in the adjoint gives the stored-C force to 1e-11 per link:
+    the two paths form C with different product kernels (the forward's table
+    loop and the local adjoint's inlined products), each accurate to ~2^-44
+    relative, so they are not bitwise equal as in the fp64 form."""
     out = []
     for recompute in (False, True):
         U = pkg.gauge_configuration(L4, start="hot", seed=13)
         P = pkg.gauge_momenta(U)
         pkg.update_momenta_(P, U, 1.0, _driver(pkg, U, 6.0, "dfloat", rho=(0.12, 0.08), recompute=recompute))
         out.append(P.to_host())
-    assert frob_mom(out[0], out[1]) < 1e-12
+    assert frob_mom(out[0], out[1]) < 1e-11
 
 
 def test_dfloat_stout_backward_matches_oracle(pkg, oracle):
@@ -156,13 +160,15 @@ def test_md_step_entry_points_validate_arguments(pkg):
 def test_hamiltonian_with_alternating_level_buffers(pkg, nlev):
     """The mixed form's Hamiltonian smears with a forward-only double-float
     stack whose levels beyond the second reuse two buffers in turn; with 3 and
-    4 levels it equals the fp64 Hamiltonian to 1e-13."""
+    4 levels it equals the fp64 Hamiltonian to 5e-13 relative (double-float
+    smearing with fixed-grid products, ~2^-44 relative per product, over 3-4
+    levels; a reused buffer holding a wrong level would be off by ~1e-3)."""
     U = pkg.gauge_configuration(L4, start="hot", seed=19)
     P = pkg.gaussian_momenta(U, seed=20)
     rho = (0.1, 0.08, 0.12, 0.1)[:nlev]
     h = {prec: pkg.md_hamiltonian(U, P, _driver(pkg, U, 6.0, prec, rho=rho)) for prec in ("fp64", "mixed", "dfloat")}
-    assert abs(h["mixed"] - h["fp64"]) <= 1e-13 * abs(h["fp64"])
-    assert abs(h["dfloat"] - h["fp64"]) <= 1e-13 * abs(h["fp64"])
+    assert abs(h["mixed"] - h["fp64"]) <= 5e-13 * abs(h["fp64"])
+    assert abs(h["dfloat"] - h["fp64"]) <= 5e-13 * abs(h["fp64"])
 
 
 def test_partial_blocks_in_every_form(pkg, oracle, exact_exp_oracle):
