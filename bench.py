@@ -63,8 +63,9 @@ def algorithmic_bytes_per_link(kclass):
     link, mat = (144, 144) if fp64 else (48, 72)
     base = _base(kclass)
     return {
-        # U in, Ubar out, C out (the double-float forward of the Hamiltonian stores no C)
-        "stout_fwd": link + link + (0 if kclass.endswith("_df") else mat),
+        # U in, Ubar out, C out (the double-float form stores C; the mixed
+        # form's forward-only Hamiltonian stack does not, so its figure is high)
+        "stout_fwd": link + link + mat,
         # U, C, Dbar in (top level: Ubar_top in); Z, Dp out -- mean of the two levels
         "bwd_local": (link + mat + mat + 2 * mat + link + mat + link + 2 * mat) / 2.0,
         # U, Z, Dp in; D out (upper level) or P read+write (bottom level) -- mean
@@ -394,6 +395,46 @@ def bench_config(L):
     V = L ** 4
     return {"workload": workload_name(L), "lattice": [L] * 4,
             "l2": "inputs larger than L2: fp64 links %d MB, momenta %d MB" % (36 * V * 16 >> 20, 32 * V * 8 >> 20)}
+
+
+def roofline_of(kern, V, L, peaks, hbm_peak, hbm_note):
+    """The HBM roofline and the compute fraction of the dominant kernel class
+    of `kern` (CUDA-event totals per class); adds share and avg_ms to `kern`.
+    Compute peaks are the cuBLAS rates measured in the run: sgemm for fp32,
+    dgemm for fp64. Double-float kernels count fp64-class flops (a 3x3
+    complex product = 198) against dgemm, and the fp32 operations those flops
+    take in the fixed-grid product (six per real multiply-add) against sgemm's
+    fp32 rate."""
+    if not kern:
+        return None, None
+    from gaugefields_gb300 import _lib as glib
+    total_ms = sum(v["ms"] for v in kern.values())
+    for k in kern:
+        kern[k]["share"] = kern[k]["ms"] / total_ms
+        kern[k]["avg_ms"] = kern[k]["ms"] / kern[k]["launches"]
+    dom = max(kern, key=lambda k: kern[k]["ms"])
+    d = kern[dom]
+    per_launch_s = d["ms"] / d["launches"] / 1e3
+    alg_bytes = algorithmic_bytes_per_link(dom) * 4 * V
+    achieved = alg_bytes / per_launch_s / 1e9
+    prec = glib.KERNEL_PRECISION[dom]
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak, "peak_note": hbm_note, "algorithmic_bytes_per_launch": alg_bytes,
+            "traffic": read_traffic(dom, L), "launches": d["launches"], "avg_launch_ms": 1e3 * per_launch_s}
+    fl = algorithmic_flops_per_link(dom) * 4 * V
+    tf = fl / per_launch_s / 1e12
+    pk = peaks["fp32_tflops"] if prec == "fp32" else peaks["fp64_tflops"]
+    note = {"fp64": "cuBLAS dgemm measured in this run", "fp32": "cuBLAS sgemm (no TF32) measured in this run",
+            "df": "double-float flops (fp64-class) against the cuBLAS dgemm rate measured in this run"}[prec]
+    compute = {"kernel": dom, "precision": prec, "achieved_tflops": tf, "peak_tflops": pk, "peak_note": note,
+               "flops_per_launch": fl, "frac": tf / pk,
+               "binding": {"fp64": "fp64 issue", "fp32": "fp32 issue / L1", "df": "fp32 issue"}[prec]}
+    if prec == "df":
+        compute["fp32_ops_tflops"] = 3.0 * tf
+        compute["fp32_frac"] = 3.0 * tf / peaks["fp32_tflops"]
+        compute["fp32_note"] = ("fp32 operations of the products (6 per real multiply-add, 3 per flop) against the "
+                                "sgemm rate")
+    return roof, compute
 
 
 def max_over_ranks(torch, dist, seconds, device):
@@ -745,30 +786,13 @@ def main():
     if not args.no_fp64:
         dh = dh_study(pkg, torch, L, args.therm, args.dh_trajectories, forms)[0]
 
-    # roofline of the dominant kernel (device time from CUDA events in the timed region)
-    roof, compute = None, None
-    if kern:
-        from gaugefields_gb300 import _lib as glib
-        dom = max(kern, key=lambda k: kern[k]["ms"])
-        d = kern[dom]
-        per_launch_s = d["ms"] / d["launches"] / 1e3
-        alg_bytes = algorithmic_bytes_per_link(dom) * 4 * V
-        achieved = alg_bytes / per_launch_s / 1e9
-        prec = glib.KERNEL_PRECISION[dom]
-        roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "peak_note": hbm_note, "algorithmic_bytes_per_launch": alg_bytes,
-                "traffic": read_traffic(dom, L), "launches": d["launches"], "avg_launch_ms": 1e3 * per_launch_s}
-        fl = algorithmic_flops_per_link(dom) * 4 * V
-        pk = peaks["fp32_tflops"] if prec == "fp32" else peaks["fp64_tflops"]
-        note = {"fp64": "cuBLAS dgemm measured in this run", "fp32": "cuBLAS sgemm (no TF32) measured in this run",
-                "df": "double-float flops (fp64-class) against the cuBLAS dgemm rate measured in this run"}[prec]
-        compute = {"kernel": dom, "precision": prec, "achieved_tflops": fl / per_launch_s / 1e12, "peak_tflops": pk,
-                   "peak_note": note, "flops_per_launch": fl, "frac": fl / per_launch_s / 1e12 / pk,
-                   "binding": {"fp64": "fp64 issue", "fp32": "fp32 issue / L1", "df": "fp32 issue"}[prec]}
-        total_ms = sum(v["ms"] for v in kern.values())
-        for k in kern:
-            kern[k]["share"] = kern[k]["ms"] / total_ms
-            kern[k]["avg_ms"] = kern[k]["ms"] / kern[k]["launches"]
+    # roofline of the dominant kernel of each form (device time from CUDA
+    # events in the timed region)
+    roof, compute = roofline_of(kern, V, L, peaks, hbm_peak, hbm_note)
+    if mixed:
+        mixed["roofline"], mixed["compute"] = roofline_of(kmx, V, L, peaks, hbm_peak, hbm_note)
+    if fp64:
+        fp64["roofline"], fp64["compute"] = roofline_of(k64, V, L, peaks, hbm_peak, hbm_note)
 
     cpu = None
     if not args.no_cpu and rank == 0:
