@@ -325,9 +325,11 @@ __constant__ DfOp c_gather_ops[10] = {
     {3, 0, 0, 0, 0, 1, 3, 0, 1, 1},  // acc += t U_k(x-k)
 };
 
-// three blocks per SM: 168 registers without spills, 36 KB of shared memory each
+// four blocks per SM: 128 registers without spills, 36 KB of shared memory
+// each; at 32^4 4.85 ms per launch against 5.42 ms with three blocks (168
+// registers) and 6.46 ms with two; five spill (96 registers)
 #ifndef GF_DF_GATHER_MINB
-#define GF_DF_GATHER_MINB 3
+#define GF_DF_GATHER_MINB 4
 #endif
 template <bool FORCE, typename EOUT>
 __global__ void __launch_bounds__(128, GF_DF_GATHER_MINB)
