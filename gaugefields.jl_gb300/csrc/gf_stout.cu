@@ -498,35 +498,52 @@ __global__ void __launch_bounds__(128, GF_DF_LOCAL_REG_MINB)
   {
     const mat3<dfl> lam = dfr_mul<false, false>(u, slot_load(sm, 1, tid));  // Lambda = U Dbar
     const cplx<dfl> trL = trace(lam), trLQ = tr_nn(lam, qh), trLQ2 = tr_nn(lam, qh2);
-    const cplx<dfl> trB1 = cc.b1[0] * trL + cc.b1[1] * trLQ + cc.b1[2] * trLQ2;
-    const cplx<dfl> trB2 = cc.b2[0] * trL + cc.b2[1] * trLQ + cc.b2[2] * trLQ2;
+    // trB_k = b_k[0] tr(Lambda) + b_k[1] tr(Lambda Qh) + b_k[2] tr(Lambda Qh^2), fixed-grid sums
+    cplx<dfl> trB[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const cplx<dfl>* b = k ? cc.b2 : cc.b1;
+      dfg_cacc t = dfg_cbegin(cabs1(b[0]) * cabs1(trL) + cabs1(b[1]) * cabs1(trLQ) + cabs1(b[2]) * cabs1(trLQ2));
+      dfg_cterm(t, b[0], trL);
+      dfg_cterm(t, b[1], trLQ);
+      dfg_cterm(t, b[2], trLQ2);
+      trB[k] = dfg_cend(t);
+    }
     // Gamma = trB1 Qh + trB2 Qh^2 + f1 Lambda + f2 (Qh Lambda + Lambda Qh)
     mat3<dfl> gam = dfr_mul<false, false>(qh, lam);
     dfr_mac<false, false>(gam, lam, qh);
+    const float m2 = cabs1(cc.f[2]), m1 = cabs1(cc.f[1]), b1 = cabs1(trB[0]), b2 = cabs1(trB[1]);
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        cplx<dfl> v = cc.f[2] * gam.e[i][j];
-        fma_(v, cc.f[1], lam.e[i][j]);
-        fma_(v, trB1, qh.e[i][j]);
-        fma_(v, trB2, qh2.e[i][j]);
-        gam.e[i][j] = v;
+        dfg_cacc v = dfg_cbegin(m2 * cabs1(gam.e[i][j]) + m1 * cabs1(lam.e[i][j]) + b1 * cabs1(qh.e[i][j]) +
+                                b2 * cabs1(qh2.e[i][j]));
+        dfg_cterm(v, cc.f[2], gam.e[i][j]);
+        dfg_cterm(v, cc.f[1], lam.e[i][j]);
+        dfg_cterm(v, trB[0], qh.e[i][j]);
+        dfg_cterm(v, trB[1], qh2.e[i][j]);
+        gam.e[i][j] = dfg_cend(v);
       }
     Y = ta_proj(times_i(dfl(-1), gam));  // Y = TA(dS/dQ), dS/dQ = -i Gamma
   }
   LinkDfn::store(Zout, mu, s, V, dfr_mul<true, false>(u, Y));  // Z = U^dag Y
   // exp(Q) = f0 + f1 Qh + f2 Qh^2;  Dp = Dbar e^Q + (Y C)^dag
   mat3<dfl> E;
+  {
+    const float m1 = cabs1(cc.f[1]), m2 = cabs1(cc.f[2]), m0 = cabs1(cc.f[0]);
+    const cplx<dfl> one = mk(dfl(1.f), dfl(0.f));
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      cplx<dfl> w = cc.f[1] * qh.e[i][j];
-      fma_(w, cc.f[2], qh2.e[i][j]);
-      if (i == j) w = w + cc.f[0];
-      E.e[i][j] = w;
-    }
+      for (int j = 0; j < 3; ++j) {
+        dfg_cacc w = dfg_cbegin(m1 * cabs1(qh.e[i][j]) + m2 * cabs1(qh2.e[i][j]) + (i == j ? m0 : 0.f));
+        dfg_cterm(w, cc.f[1], qh.e[i][j]);
+        dfg_cterm(w, cc.f[2], qh2.e[i][j]);
+        if (i == j) dfg_cterm(w, cc.f[0], one);
+        E.e[i][j] = dfg_cend(w);
+      }
+  }
   mat3<dfl> dp = dfr_mul<false, false>(slot_load(sm, 1, tid), E);
   dfr_mac<true, true>(dp, slot_load(sm, 0, tid), Y);
   LinkDfn::store(Dpout, mu, s, V, dp);

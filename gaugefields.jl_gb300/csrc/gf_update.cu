@@ -34,10 +34,10 @@ __global__ void __launch_bounds__(128) k_link_update(const double2* Uin, double2
   // re-unitarisation rebuilds row 3 from rows 1-2, so only those are formed
   mat3<R> w;
   if (reunit) {
-    w = mul_nn_rows12(expiq<R, 2>(q), u);
+    w = mul_nn_rows12(expiq<R, 2, true>(q), u);
     reunitarize(w);
   } else {
-    w = mul_nn(expiq(q), u);
+    w = mul_nn(expiq<R, 3, true>(q), u);
   }
   LinkFull<R>::store(Uout, mu, s, V, w);
   if (sh32) {

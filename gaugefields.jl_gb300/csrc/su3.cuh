@@ -585,26 +585,38 @@ GF_HD void herm_invariants(const mat3<R>& q, R& c0, R& c1) {
   c0 = q11 * q22 * q33 + R(2) * re3 - q11 * a23 - q22 * a13 - q33 * a12;
 }
 
+// Entry (i,j) of f0 + f1 Q + f2 Q^2 with the type's operators
+template <typename R>
+__device__ __forceinline__ cplx<R> ch_combine_ops(const ch_coef<R>& cc, const mat3<R>& q, const mat3<R>& q2, int i,
+                                                  int j) {
+  cplx<R> v = cc.f[1] * q.e[i][j];
+  fma_(v, cc.f[2], q2.e[i][j]);
+  if (i == j) v = v + cc.f[0];
+  return v;
+}
+template <typename R>
+__device__ __forceinline__ cplx<R> ch_combine(const ch_coef<R>& cc, const mat3<R>& q, const mat3<R>& q2, int i, int j) {
+  return ch_combine_ops(cc, q, q2, i, j);
+}
 // exp(iQ) for traceless Hermitian Q. Q2 receives Q^2 (callers reuse it).
 // ROWS = 2 forms rows 1-2 only (row 3 left zero), for products whose row 3 is
-// rebuilt or not stored.
-template <typename R, int ROWS = 3>
+// rebuilt or not stored. OPS = true combines f0 + f1 Q + f2 Q^2 with the
+// type's operators (for double-float: the accurate double-word sums, ~2^-48,
+// which chains of link updates keep to 1e-12 of fp64), false with the
+// fixed-grid sum (~2^-44 of the bound) where one is given.
+template <typename R, int ROWS = 3, bool OPS = false>
 __device__ __forceinline__ mat3<R> expiq(const mat3<R>& q, mat3<R>* q2out = nullptr) {
   R c0, c1;
   herm_invariants(q, c0, c1);
   ch_coef<R> cc;
   ch_coefficients<R, false>(c0, c1, cc);
-  mat3<R> q2 = herm_square(q);
+  // OPS: the generic (operator) square as well; otherwise the type's best
+  mat3<R> q2 = OPS ? herm_square<R>(q) : herm_square(q);
   mat3<R> e = zero3<R>();
 #pragma unroll
   for (int i = 0; i < ROWS; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      cplx<R> v = cc.f[1] * q.e[i][j];
-      fma_(v, cc.f[2], q2.e[i][j]);
-      if (i == j) v = v + cc.f[0];
-      e.e[i][j] = v;
-    }
+    for (int j = 0; j < 3; ++j) e.e[i][j] = OPS ? ch_combine_ops(cc, q, q2, i, j) : ch_combine(cc, q, q2, i, j);
   if (q2out) *q2out = q2;
   return e;
 }
@@ -769,6 +781,115 @@ GF_HD mat3<dfl> dfg_matmul(const mat3<dfl>& a, const mat3<dfl>& b, const mat3<df
       r.e[i][j] = mk(df_fast_two_sum(Ar - K, Lr), df_fast_two_sum(Ai - K, Li));
     }
   return r;
+}
+
+// Fixed-grid accumulators for single sums of products (traces, Q^2 and the
+// coefficient combinations of the stout adjoint): the same grid scheme as
+// dfg_matmul, with the bound M on |partial sums| given by the caller (sums
+// of |x||y| over the terms, from the fp32 high parts; |x| of a complex value
+// bounded by |re| + |im|). About 28 fp32 operations per complex multiply-add
+// against ~110 through the double-float operators.
+struct dfg_acc {
+  float K, A, L;
+};
+struct dfg_cacc {
+  float K, Ar, Ai, Lr, Li;
+};
+GF_HD float cabs1(const cplx<dfl>& x) { return fabsf(x.re.hi) + fabsf(x.im.hi); }
+GF_HD dfg_acc dfg_begin(float M) {
+  const float K = df_grid_const(M * M);
+  return dfg_acc{K, K, 0.f};
+}
+GF_HD dfg_cacc dfg_cbegin(float M) {
+  const float K = df_grid_const(M * M);
+  return dfg_cacc{K, K, K, 0.f, 0.f};
+}
+// real += x y
+GF_HD void dfg_term(dfg_acc& a, dfl x, dfl y) { grid_term(a.A, a.L, x.hi, x.lo, y.hi, y.lo); }
+// complex += x y
+GF_HD void dfg_cterm(dfg_cacc& a, const cplx<dfl>& x, const cplx<dfl>& y) {
+  grid_term(a.Ar, a.Lr, x.re.hi, x.re.lo, y.re.hi, y.re.lo);
+  grid_term(a.Ar, a.Lr, -x.im.hi, -x.im.lo, y.im.hi, y.im.lo);
+  grid_term(a.Ai, a.Li, x.re.hi, x.re.lo, y.im.hi, y.im.lo);
+  grid_term(a.Ai, a.Li, x.im.hi, x.im.lo, y.re.hi, y.re.lo);
+}
+// complex += r y with r real
+GF_HD void dfg_rcterm(dfg_cacc& a, dfl r, const cplx<dfl>& y) {
+  grid_term(a.Ar, a.Lr, r.hi, r.lo, y.re.hi, y.re.lo);
+  grid_term(a.Ai, a.Li, r.hi, r.lo, y.im.hi, y.im.lo);
+}
+// real part += c
+GF_HD void dfg_cadd_re(dfg_cacc& a, dfl c) { grid_term(a.Ar, a.Lr, c.hi, c.lo, 1.f, 0.f); }
+GF_HD dfl dfg_end(const dfg_acc& a) { return df_fast_two_sum(a.A - a.K, a.L); }
+GF_HD cplx<dfl> dfg_cend(const dfg_cacc& a) {
+  return mk(df_fast_two_sum(a.Ar - a.K, a.Lr), df_fast_two_sum(a.Ai - a.K, a.Li));
+}
+
+// tr(A B) for double-float matrices, one fixed-grid sum
+__device__ __forceinline__ cplx<dfl> tr_nn(const mat3<dfl>& a, const mat3<dfl>& b) {
+  float M = 0.f;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) M = fmaf(cabs1(a.e[i][k]), cabs1(b.e[k][i]), M);
+  dfg_cacc acc = dfg_cbegin(M);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) dfg_cterm(acc, a.e[i][k], b.e[k][i]);
+  return dfg_cend(acc);
+}
+
+// Q^2 of a Hermitian double-float Q with fixed-grid sums
+__device__ __forceinline__ mat3<dfl> herm_square(const mat3<dfl>& q) {
+  mat3<dfl> r;
+  float a[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) a[i][k] = cabs1(q.e[i][k]);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    float M = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) M = fmaf(a[i][k], a[i][k], M);
+    dfg_acc d = dfg_begin(M);
+    dfg_term(d, q.e[i][i].re, q.e[i][i].re);
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      if (k != i) {
+        dfg_term(d, q.e[i][k].re, q.e[i][k].re);
+        dfg_term(d, q.e[i][k].im, q.e[i][k].im);
+      }
+    r.e[i][i] = mk(dfg_end(d), dfl(0.f));
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = i + 1; j < 3; ++j) {
+      // sum_k Q_ik Q_kj with Q_ii, Q_jj real
+      const int k = 3 - i - j;
+      const float M = (a[i][i] + a[j][j]) * a[i][j] + a[i][k] * a[k][j];
+      dfg_cacc v = dfg_cbegin(M);
+      dfg_rcterm(v, q.e[i][i].re, q.e[i][j]);
+      dfg_rcterm(v, q.e[j][j].re, q.e[i][j]);
+      dfg_cterm(v, q.e[i][k], q.e[k][j]);
+      r.e[i][j] = dfg_cend(v);
+      r.e[j][i] = conj(r.e[i][j]);
+    }
+  return r;
+}
+
+// f0 + f1 Q + f2 Q^2 (ch_combine, found by argument-dependent lookup from expiq):
+// the double-float entry as one fixed-grid sum
+__device__ __forceinline__ cplx<dfl> ch_combine(const ch_coef<dfl>& cc, const mat3<dfl>& q, const mat3<dfl>& q2,
+                                                int i, int j) {
+  dfg_cacc w = dfg_cbegin(cabs1(cc.f[1]) * cabs1(q.e[i][j]) + cabs1(cc.f[2]) * cabs1(q2.e[i][j]) +
+                          (i == j ? cabs1(cc.f[0]) : 0.f));
+  dfg_cterm(w, cc.f[1], q.e[i][j]);
+  dfg_cterm(w, cc.f[2], q2.e[i][j]);
+  if (i == j) dfg_cterm(w, cc.f[0], mk(dfl(1.f), dfl(0.f)));
+  return dfg_cend(w);
 }
 
 // Rows 1-2 of A*B (row 3 left zero), for updates that re-unitarise right
