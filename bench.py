@@ -41,8 +41,9 @@ L2_BYTES = 129 * 1024 * 1024
 HEADLINE_FORM = "dfloat"
 
 
-def workload_name(L):
-    return "%d^4 SU(3) HMC, Wilson beta=6.0 on 2-level stout (rho=0.1) links, tau=1, 20 QPQ steps, Haar start seed 7" % L
+def workload_name(L, steps=NSTEPS):
+    return ("%d^4 SU(3) HMC, Wilson beta=6.0 on 2-level stout (rho=0.1) links, tau=1, %d QPQ steps, Haar start seed 7"
+            % (L, steps))
 
 
 # ---------------------------------------------------------------------------
@@ -501,7 +502,7 @@ def run_precision_mode(args):
     L = args.lattice
     forms = ("fp64",) + (() if args.no_mixed else ("mixed",)) + (() if args.no_dfloat else ("dfloat",))
     out, rows = dh_study(pkg, torch, L, args.therm, args.steps, forms, args.md_steps, start="hot", progress=True)
-    out = dict({"mode": "precision", "workload": workload_name(L), "therm": args.therm}, **out)
+    out = dict({"mode": "precision", "workload": workload_name(L, args.md_steps or NSTEPS), "therm": args.therm}, **out)
     out["rows"] = rows
     print(json.dumps(out))
     return 0

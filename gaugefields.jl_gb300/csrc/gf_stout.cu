@@ -459,6 +459,47 @@ __device__ __forceinline__ mat3<dfl> staple_sum_dfr(const E* __restrict__ U, int
   return S;
 }
 
+// The coefficient algebra of the double-float local adjoint, as fixed-grid
+// sums: on entry gam holds Qh Lambda + Lambda Qh; on exit
+//   gam = f2 (Qh Lambda + Lambda Qh) + f1 Lambda + trB1 Qh + trB2 Qh^2,
+//   E   = f0 + f1 Qh + f2 Qh^2 = exp(Q),
+// with trB_k = b_k[0] tr(Lambda) + b_k[1] tr(Lambda Qh) + b_k[2] tr(Lambda Qh^2)
+// (CdexpQdQ!, src/smearing/stout_fast.jl:888-946).
+__device__ __forceinline__ void df_gamma_and_exp(const ch_coef<dfl>& cc, const mat3<dfl>& lam, const mat3<dfl>& qh,
+                                                 const mat3<dfl>& qh2, mat3<dfl>& gam, mat3<dfl>& E) {
+  const cplx<dfl> trL = trace(lam), trLQ = tr_nn(lam, qh), trLQ2 = tr_nn(lam, qh2);
+  cplx<dfl> trB[2];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const cplx<dfl>* b = k ? cc.b2 : cc.b1;
+    dfg_cacc t = dfg_cbegin(cabs1(b[0]) * cabs1(trL) + cabs1(b[1]) * cabs1(trLQ) + cabs1(b[2]) * cabs1(trLQ2));
+    dfg_cterm(t, b[0], trL);
+    dfg_cterm(t, b[1], trLQ);
+    dfg_cterm(t, b[2], trLQ2);
+    trB[k] = dfg_cend(t);
+  }
+  const float m2 = cabs1(cc.f[2]), m1 = cabs1(cc.f[1]), m0 = cabs1(cc.f[0]);
+  const float b1 = cabs1(trB[0]), b2 = cabs1(trB[1]);
+  const cplx<dfl> one = mk(dfl(1.f), dfl(0.f));
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      dfg_cacc v = dfg_cbegin(m2 * cabs1(gam.e[i][j]) + m1 * cabs1(lam.e[i][j]) + b1 * cabs1(qh.e[i][j]) +
+                              b2 * cabs1(qh2.e[i][j]));
+      dfg_cterm(v, cc.f[2], gam.e[i][j]);
+      dfg_cterm(v, cc.f[1], lam.e[i][j]);
+      dfg_cterm(v, trB[0], qh.e[i][j]);
+      dfg_cterm(v, trB[1], qh2.e[i][j]);
+      gam.e[i][j] = dfg_cend(v);
+      dfg_cacc w = dfg_cbegin(m1 * cabs1(qh.e[i][j]) + m2 * cabs1(qh2.e[i][j]) + (i == j ? m0 : 0.f));
+      dfg_cterm(w, cc.f[1], qh.e[i][j]);
+      dfg_cterm(w, cc.f[2], qh2.e[i][j]);
+      if (i == j) dfg_cterm(w, cc.f[0], one);
+      E.e[i][j] = dfg_cend(w);
+    }
+}
+
 // The local adjoint with products in registers (the register form of
 // k_bwd_local_df, same order of operations). C and Dbar wait in two
 // per-thread shared-memory slots between their uses, which keeps the kernel
@@ -494,56 +535,17 @@ __global__ void __launch_bounds__(128, GF_DF_LOCAL_REG_MINB)
   ch_coef<dfl> cc;
   ch_coefficients<dfl, true>(c0, c1, cc);
   const mat3<dfl> qh2 = herm_square(qh);
-  mat3<dfl> Y;
+  mat3<dfl> Y, E;
   {
     const mat3<dfl> lam = dfr_mul<false, false>(u, slot_load(sm, 1, tid));  // Lambda = U Dbar
-    const cplx<dfl> trL = trace(lam), trLQ = tr_nn(lam, qh), trLQ2 = tr_nn(lam, qh2);
-    // trB_k = b_k[0] tr(Lambda) + b_k[1] tr(Lambda Qh) + b_k[2] tr(Lambda Qh^2), fixed-grid sums
-    cplx<dfl> trB[2];
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      const cplx<dfl>* b = k ? cc.b2 : cc.b1;
-      dfg_cacc t = dfg_cbegin(cabs1(b[0]) * cabs1(trL) + cabs1(b[1]) * cabs1(trLQ) + cabs1(b[2]) * cabs1(trLQ2));
-      dfg_cterm(t, b[0], trL);
-      dfg_cterm(t, b[1], trLQ);
-      dfg_cterm(t, b[2], trLQ2);
-      trB[k] = dfg_cend(t);
-    }
-    // Gamma = trB1 Qh + trB2 Qh^2 + f1 Lambda + f2 (Qh Lambda + Lambda Qh)
+    // Gamma = trB1 Qh + trB2 Qh^2 + f1 Lambda + f2 (Qh Lambda + Lambda Qh); E = exp(Q)
     mat3<dfl> gam = dfr_mul<false, false>(qh, lam);
     dfr_mac<false, false>(gam, lam, qh);
-    const float m2 = cabs1(cc.f[2]), m1 = cabs1(cc.f[1]), b1 = cabs1(trB[0]), b2 = cabs1(trB[1]);
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        dfg_cacc v = dfg_cbegin(m2 * cabs1(gam.e[i][j]) + m1 * cabs1(lam.e[i][j]) + b1 * cabs1(qh.e[i][j]) +
-                                b2 * cabs1(qh2.e[i][j]));
-        dfg_cterm(v, cc.f[2], gam.e[i][j]);
-        dfg_cterm(v, cc.f[1], lam.e[i][j]);
-        dfg_cterm(v, trB[0], qh.e[i][j]);
-        dfg_cterm(v, trB[1], qh2.e[i][j]);
-        gam.e[i][j] = dfg_cend(v);
-      }
+    df_gamma_and_exp(cc, lam, qh, qh2, gam, E);
     Y = ta_proj(times_i(dfl(-1), gam));  // Y = TA(dS/dQ), dS/dQ = -i Gamma
   }
   LinkDfn::store(Zout, mu, s, V, dfr_mul<true, false>(u, Y));  // Z = U^dag Y
-  // exp(Q) = f0 + f1 Qh + f2 Qh^2;  Dp = Dbar e^Q + (Y C)^dag
-  mat3<dfl> E;
-  {
-    const float m1 = cabs1(cc.f[1]), m2 = cabs1(cc.f[2]), m0 = cabs1(cc.f[0]);
-    const cplx<dfl> one = mk(dfl(1.f), dfl(0.f));
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        dfg_cacc w = dfg_cbegin(m1 * cabs1(qh.e[i][j]) + m2 * cabs1(qh2.e[i][j]) + (i == j ? m0 : 0.f));
-        dfg_cterm(w, cc.f[1], qh.e[i][j]);
-        dfg_cterm(w, cc.f[2], qh2.e[i][j]);
-        if (i == j) dfg_cterm(w, cc.f[0], one);
-        E.e[i][j] = dfg_cend(w);
-      }
-  }
+  // Dp = Dbar e^Q + (Y C)^dag
   mat3<dfl> dp = dfr_mul<false, false>(slot_load(sm, 1, tid), E);
   dfr_mac<true, true>(dp, slot_load(sm, 0, tid), Y);
   LinkDfn::store(Dpout, mu, s, V, dp);
@@ -641,24 +643,8 @@ __global__ void __launch_bounds__(128, GF_MINB_ADJ(dfl))
     if (q == 27) {
       const mat3<dfl> lam = slot_load(sm, 3, tid), qh = slot_load(sm, 1, tid), qh2 = slot_load(sm, 2, tid);
       mat3<dfl> gam = slot_load(sm, 0, tid);
-      const cplx<dfl> trL = trace(lam), trLQ = tr_nn(lam, qh), trLQ2 = tr_nn(lam, qh2);
-      const cplx<dfl> trB1 = cc.b1[0] * trL + cc.b1[1] * trLQ + cc.b1[2] * trLQ2;
-      const cplx<dfl> trB2 = cc.b2[0] * trL + cc.b2[1] * trLQ + cc.b2[2] * trLQ2;
       mat3<dfl> E;
-#pragma unroll
-      for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-          cplx<dfl> v = cc.f[2] * gam.e[i][j];
-          fma_(v, cc.f[1], lam.e[i][j]);
-          fma_(v, trB1, qh.e[i][j]);
-          fma_(v, trB2, qh2.e[i][j]);
-          gam.e[i][j] = v;
-          cplx<dfl> w = cc.f[1] * qh.e[i][j];
-          fma_(w, cc.f[2], qh2.e[i][j]);
-          if (i == j) w = w + cc.f[0];
-          E.e[i][j] = w;
-        }
+      df_gamma_and_exp(cc, lam, qh, qh2, gam, E);
       slot_store(sm, 0, tid, ta_proj(times_i(dfl(-1), gam)));  // Y
       slot_store(sm, 2, tid, E);                                // e^Q
     }

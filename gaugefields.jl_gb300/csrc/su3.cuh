@@ -461,6 +461,50 @@ struct ch_state {
   }
 };
 
+// One term of the series with the phase i^n split into its target (odd n:
+// the imaginary part, even n: the real part; compile-time ODD) and its sign
+// ((n & 2) ? -1 : +1, at run time), so a loop over pairs of terms holds two
+// step bodies instead of four (the double-float kernels are instruction-fetch
+// bound).
+template <typename R, bool DERIV, bool ODD>
+struct ch_pair_state {
+  typedef ch_ops<R> O;
+  static __device__ __forceinline__ typename O::mag_t step(int n, R c0, R c1, R& a, R& b, R& c, R& a0, R& b0,
+                                                          R& c0d, R& a1, R& b1, R& c1d, R* fr, R* fi, R* d1r,
+                                                          R* d1i, R* d2r, R* d2i) {
+    R na = c0 * c, nb = O::sum(a, c1 * c), nc = b;
+    R na0 = 0, nb0 = 0, nc0 = 0, na1 = 0, nb1 = 0, nc1 = 0;
+    if (DERIV) {
+      na0 = O::sum(c, c0 * c0d);
+      nb0 = O::sum(a0, c1 * c0d);
+      nc0 = b0;
+      na1 = c0 * c1d;
+      nb1 = O::sum(O::sum(a1, c), c1 * c1d);
+      nc1 = b1;
+    }
+    a = na; b = nb; c = nc;
+    R fact = inv_fact<R>(n);
+    if (n & 2) fact = -fact;
+    const R t[3] = {a * fact, b * fact, c * fact};
+    typename O::mag_t mag = O::mag(t[0]) + O::mag(t[1]) + O::mag(t[2]);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) O::add(ODD ? fi[j] : fr[j], t[j]);
+    if (DERIV) {
+      a0 = na0; b0 = nb0; c0d = nc0;
+      a1 = na1; b1 = nb1; c1d = nc1;
+      const R u0[3] = {a0 * fact, b0 * fact, c0d * fact};
+      const R u1[3] = {a1 * fact, b1 * fact, c1d * fact};
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        O::add(ODD ? d2i[j] : d2r[j], u0[j]);
+        O::add(ODD ? d1i[j] : d1r[j], u1[j]);
+      }
+      mag += O::mag(u0[0]) + O::mag(u0[1]) + O::mag(u0[2]) + O::mag(u1[0]) + O::mag(u1[1]) + O::mag(u1[2]);
+    }
+    return mag;
+  }
+};
+
 // Double-float form: the terms are summed in double-float while the last
 // term of a group of four is at least 1e-8; the rest of the series, terms
 // below 1e-8, runs in fp32 (its rounding, ~1e-7 of the tail, is below 1e-15
@@ -474,32 +518,27 @@ __device__ __forceinline__ void ch_coefficients_df(dfl c0, dfl c1, ch_coef<dfl>&
   dfl fr[3] = {dfl(1.f), dfl(0.f), dfl(0.f)}, fi[3] = {0, 0, 0};
   dfl d1r[3] = {0, 0, 0}, d1i[3] = {0, 0, 0}, d2r[3] = {0, 0, 0}, d2i[3] = {0, 0, 0};
   int n = 1;
-  for (; n + 3 < GF_CH_TERMS; n += 4) {
-    ch_state<dfl, DERIV, 1>::step(n, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
-    ch_state<dfl, DERIV, 2>::step(n + 1, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
-    ch_state<dfl, DERIV, 3>::step(n + 2, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
-    const float mag =
-        ch_state<dfl, DERIV, 0>::step(n + 3, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
+  for (; n + 1 < GF_CH_TERMS; n += 2) {
+    ch_pair_state<dfl, DERIV, true>::step(n, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr, fi, d1r, d1i, d2r, d2i);
+    const float mag = ch_pair_state<dfl, DERIV, false>::step(n + 1, c0, c1, a, b, c, a0, b0, c0d, a1, b1, c1d, fr,
+                                                              fi, d1r, d1i, d2r, d2i);
     if (mag < 1.0e-8f) {
-      n += 4;
+      n += 2;
       break;
     }
   }
-  // fp32 tail from term n (n = 1 mod 4, so the phases continue in order)
+  // fp32 tail from term n (n odd, so the pairs continue in order)
   float fa = a.hi + a.lo, fb = b.hi + b.lo, fc = c.hi + c.lo;
   float fa0 = a0.hi + a0.lo, fb0 = b0.hi + b0.lo, fc0 = c0d.hi + c0d.lo;
   float fa1 = a1.hi + a1.lo, fb1 = b1.hi + b1.lo, fc1 = c1d.hi + c1d.lo;
   const float g0 = c0.hi + c0.lo, g1 = c1.hi + c1.lo;
   float tr[3] = {0.f, 0.f, 0.f}, ti[3] = {0.f, 0.f, 0.f};
   float e1r[3] = {0.f, 0.f, 0.f}, e1i[3] = {0.f, 0.f, 0.f}, e2r[3] = {0.f, 0.f, 0.f}, e2i[3] = {0.f, 0.f, 0.f};
-  for (; n + 3 < GF_CH_TERMS; n += 4) {
-    ch_state<float, DERIV, 1>::step(n, g0, g1, fa, fb, fc, fa0, fb0, fc0, fa1, fb1, fc1, tr, ti, e1r, e1i, e2r, e2i);
-    ch_state<float, DERIV, 2>::step(n + 1, g0, g1, fa, fb, fc, fa0, fb0, fc0, fa1, fb1, fc1, tr, ti, e1r, e1i, e2r,
-                                    e2i);
-    ch_state<float, DERIV, 3>::step(n + 2, g0, g1, fa, fb, fc, fa0, fb0, fc0, fa1, fb1, fc1, tr, ti, e1r, e1i, e2r,
-                                    e2i);
-    const float mag = ch_state<float, DERIV, 0>::step(n + 3, g0, g1, fa, fb, fc, fa0, fb0, fc0, fa1, fb1, fc1, tr, ti,
-                                                      e1r, e1i, e2r, e2i);
+  for (; n + 1 < GF_CH_TERMS; n += 2) {
+    ch_pair_state<float, DERIV, true>::step(n, g0, g1, fa, fb, fc, fa0, fb0, fc0, fa1, fb1, fc1, tr, ti, e1r, e1i,
+                                            e2r, e2i);
+    const float mag = ch_pair_state<float, DERIV, false>::step(n + 1, g0, g1, fa, fb, fc, fa0, fb0, fc0, fa1, fb1,
+                                                                fc1, tr, ti, e1r, e1i, e2r, e2i);
     if (mag < 2.0e-16f) break;
   }
 #pragma unroll
