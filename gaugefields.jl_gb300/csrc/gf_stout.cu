@@ -371,17 +371,6 @@ __global__ void __launch_bounds__(128, GF_DF_GATHER_MINB)
   }
 }
 
-// Fixed-grid double-float products with compile-time operand forms (the
-// register-resident kernels below)
-template <bool DA, bool DB>
-__device__ __forceinline__ mat3<dfl> dfr_mul(const mat3<dfl>& a, const mat3<dfl>& b) {
-  return dfg_matmul<DA, DB, false>(a, b, nullptr);
-}
-template <bool DA, bool DB>
-__device__ __forceinline__ void dfr_mac(mat3<dfl>& acc, const mat3<dfl>& a, const mat3<dfl>& b) {
-  acc = dfg_matmul<DA, DB, true>(a, b, &acc);
-}
-
 // The stout forward: F0 = U, d0 = mu, d1 = nu; sites x, x+mu, x+nu,
 // x+mu-nu, x-nu; slot 0 = t, slot 1 = acc. Ops 0-3 (per nu) build S_mu in
 // dS/dU order as add_staple_pair does; op 4 forms U S; op 5 e^Q U.
@@ -435,30 +424,6 @@ __global__ void __launch_bounds__(128, GF_DF_FWD_MINB)
   if (live) LinkDfn::store(Uout, mu, s, V, slot_load(sm, 1, tid));
 }
 
-// S_mu(x) (the six staples in dS/dU order, as staple_sum) with fixed-grid
-// double-float products, from either storage
-template <typename E>
-__device__ __forceinline__ mat3<dfl> staple_sum_dfr(const E* __restrict__ U, int mu, const Geom& g, const Site& st,
-                                                    int s) {
-  const int V = g.vol;
-  const int xpm = nbr_rt(g, st, mu, +1);
-  mat3<dfl> S = zero3<dfl>();
-#pragma unroll 1
-  for (int k = 1; k < 4; ++k) {
-    const int nu = (mu + k) & 3;
-    const int xpn = nbr_rt(g, st, nu, +1);
-    const int xmn = nbr_rt(g, st, nu, -1);
-    const int xpm_mn = nbr2_rt(g, st, mu, +1, nu, -1);
-    // up: U_nu(x+mu) U_mu(x+nu)^dag U_nu(x)^dag
-    mat3<dfl> t = dfr_mul<false, true>(DfIO<E>::load(U, nu, xpm, V), DfIO<E>::load(U, mu, xpn, V));
-    dfr_mac<false, true>(S, t, DfIO<E>::load(U, nu, s, V));
-    // down: U_nu(x+mu-nu)^dag U_mu(x-nu)^dag U_nu(x-nu)
-    t = dfr_mul<true, true>(DfIO<E>::load(U, nu, xpm_mn, V), DfIO<E>::load(U, mu, xmn, V));
-    dfr_mac<false, false>(S, t, DfIO<E>::load(U, nu, xmn, V));
-  }
-  return S;
-}
-
 // The coefficient algebra of the double-float local adjoint, as fixed-grid
 // sums: on entry gam holds Qh Lambda + Lambda Qh; on exit
 //   gam = f2 (Qh Lambda + Lambda Qh) + f1 Lambda + trB1 Qh + trB2 Qh^2,
@@ -499,66 +464,6 @@ __device__ __forceinline__ void df_gamma_and_exp(const ch_coef<dfl>& cc, const m
       E.e[i][j] = dfg_cend(w);
     }
 }
-
-// The local adjoint with products in registers (the register form of
-// k_bwd_local_df, same order of operations). C and Dbar wait in two
-// per-thread shared-memory slots between their uses, which keeps the kernel
-// within the register file.
-#ifndef GF_DF_LOCAL_REG_MINB
-#define GF_DF_LOCAL_REG_MINB 2
-#endif
-template <bool TOP>
-__global__ void __launch_bounds__(128, GF_DF_LOCAL_REG_MINB)
-    k_bwd_local_dfr(const float4* __restrict__ U, const float4* __restrict__ F1, const float4* __restrict__ Cst,
-                    float4* __restrict__ Zout, float4* __restrict__ Dpout, Geom g, dfl rho, dfl halfbeta) {
-  __shared__ __align__(16) float sm[2 * 36 * 128];
-  const int tid = threadIdx.x;
-  int s, mu;
-  link_of_thread(s, mu);
-  if (s >= g.vol) return;  // the slots are per thread: no block-wide synchronisation
-  const int V = g.vol;
-  const Site st = site_of(g, s);
-  {
-    const mat3<dfl> C = Cst ? LinkDfn::load(Cst, mu, s, V) : scale(rho, dag(staple_sum_dfr(U, mu, g, st, s)));
-    slot_store(sm, 0, tid, C);
-  }
-  {
-    // top level: Dbar = beta/2 S(Ubar_top)
-    const mat3<dfl> db = TOP ? scale(halfbeta, staple_sum_dfr(F1, mu, g, st, s)) : LinkDfn::load(F1, mu, s, V);
-    slot_store(sm, 1, tid, db);
-  }
-  const mat3<dfl> u = LinkDfn::load(U, mu, s, V);
-  // Qh = -i TA(C U^dag)
-  const mat3<dfl> qh = times_i(dfl(-1), ta_proj(dfr_mul<false, true>(slot_load(sm, 0, tid), u)));
-  dfl c0, c1;
-  herm_invariants(qh, c0, c1);
-  ch_coef<dfl> cc;
-  ch_coefficients<dfl, true>(c0, c1, cc);
-  const mat3<dfl> qh2 = herm_square(qh);
-  mat3<dfl> Y, E;
-  {
-    const mat3<dfl> lam = dfr_mul<false, false>(u, slot_load(sm, 1, tid));  // Lambda = U Dbar
-    // Gamma = trB1 Qh + trB2 Qh^2 + f1 Lambda + f2 (Qh Lambda + Lambda Qh); E = exp(Q)
-    mat3<dfl> gam = dfr_mul<false, false>(qh, lam);
-    dfr_mac<false, false>(gam, lam, qh);
-    df_gamma_and_exp(cc, lam, qh, qh2, gam, E);
-    Y = ta_proj(times_i(dfl(-1), gam));  // Y = TA(dS/dQ), dS/dQ = -i Gamma
-  }
-  LinkDfn::store(Zout, mu, s, V, dfr_mul<true, false>(u, Y));  // Z = U^dag Y
-  // Dp = Dbar e^Q + (Y C)^dag
-  mat3<dfl> dp = dfr_mul<false, false>(slot_load(sm, 1, tid), E);
-  dfr_mac<true, true>(dp, slot_load(sm, 0, tid), Y);
-  LinkDfn::store(Dpout, mu, s, V, dp);
-}
-
-// the local adjoint form: 1 registers (k_bwd_local_dfr), 0 the table loop.
-// At 32^4 the register form takes 7.7 ms per launch, the table loop 8.0 ms.
-// For the forward and the gather the table loop is faster (4.1 against 4.5 ms,
-// 5.8 against 8.8 ms): their register forms inline 14 and 10 products per
-// loop body and run two blocks per SM (255 registers) against three.
-#ifndef GF_DF_LOCAL_REG
-#define GF_DF_LOCAL_REG 1
-#endif
 
 // The local adjoint: F0 = U, F1 = Dbar (or the top level's smeared links),
 // F2 = the stored C; d0 = mu, d1 = nu; sites x, x+mu, x+nu, x+mu-nu, x-nu.
@@ -806,17 +711,11 @@ static void backward_df(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, doub
     {
       ProfScope prof(ctx, GF_K_BWD_LOCAL_DF);
       const float4* f1 = top ? (const float4*)st->lev_in[l + 1]->ptr : din;
-      if (GF_DF_LOCAL_REG) {
-        auto kern = top ? k_bwd_local_dfr<true> : k_bwd_local_dfr<false>;
-        kern<<<grid, 128, 0, ctx->stream>>>(u, f1, Cst, (float4*)st->Z->ptr, (float4*)st->Dp->ptr, ctx->geom,
-                                            (dfl)st->rho[l], (dfl)(0.5 * beta));
-      } else {
-        const size_t smem = (size_t)GF_LOCAL_SLOTS * 36 * 128 * sizeof(float);
-        auto kern = top ? k_bwd_local_df<true> : k_bwd_local_df<false>;
-        GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kern<<<grid, 128, smem, ctx->stream>>>(u, f1, Cst, (float4*)st->Z->ptr, (float4*)st->Dp->ptr, ctx->geom,
-                                               (dfl)st->rho[l], (dfl)(0.5 * beta));
-      }
+      const size_t smem = (size_t)GF_LOCAL_SLOTS * 36 * 128 * sizeof(float);
+      auto kern = top ? k_bwd_local_df<true> : k_bwd_local_df<false>;
+      GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      kern<<<grid, 128, smem, ctx->stream>>>(u, f1, Cst, (float4*)st->Z->ptr, (float4*)st->Dp->ptr, ctx->geom,
+                                             (dfl)st->rho[l], (dfl)(0.5 * beta));
       GF_CHECK_LAUNCH();
     }
     if (dsdrho) dsdrho[l] = level_dsdrho(ctx, st, l);
