@@ -495,8 +495,13 @@ __constant__ DfOp c_local_ops[31] = {
     {14, 0, 0, 1, 3, 0, 0, 1, 3, 1},  // 30: Dp += C^dag Y^dag
 };
 
+// Blocks per SM of the local adjoint below the top level: its slots 0-3
+// (72 KB) let three blocks share an SM; the top level also needs slot 4.
+#ifndef GF_DF_LOCAL_MINB_LOWER
+#define GF_DF_LOCAL_MINB_LOWER 3
+#endif
 template <bool TOP>
-__global__ void __launch_bounds__(128, GF_MINB_ADJ(dfl))
+__global__ void __launch_bounds__(128, TOP ? GF_MINB_ADJ(dfl) : GF_DF_LOCAL_MINB_LOWER)
     k_bwd_local_df(const float4* __restrict__ U, const float4* __restrict__ F1, const float4* __restrict__ Cst,
                    float4* __restrict__ Zout, float4* __restrict__ Dpout, Geom g, dfl rho, dfl halfbeta) {
   extern __shared__ float sm[];  // GF_LOCAL_SLOTS slots of 36 x 128 floats
@@ -711,7 +716,9 @@ static void backward_df(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, doub
     {
       ProfScope prof(ctx, GF_K_BWD_LOCAL_DF);
       const float4* f1 = top ? (const float4*)st->lev_in[l + 1]->ptr : din;
-      const size_t smem = (size_t)GF_LOCAL_SLOTS * 36 * 128 * sizeof(float);
+      // slots used: 0-3, 4 (the top level's Dbar), 5 (a recomputed C)
+      const int nslots = Cst == nullptr ? GF_LOCAL_SLOTS : (top ? 5 : 4);
+      const size_t smem = (size_t)nslots * 36 * 128 * sizeof(float);
       auto kern = top ? k_bwd_local_df<true> : k_bwd_local_df<false>;
       GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       kern<<<grid, 128, smem, ctx->stream>>>(u, f1, Cst, (float4*)st->Z->ptr, (float4*)st->Dp->ptr, ctx->geom,

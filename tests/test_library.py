@@ -198,6 +198,23 @@ def test_double_float_op_tables_stay_in_bounds():
     # the placeholders resolve to fields 1, 2 or slots 4, 5 (src 7, 8)
     assert "recompute ? 8 : 2" in src and "TOP ? 7 : 1" in src
     assert nslots["c_local_ops"] >= 6
+    # the local adjoint's shared memory is sized per launch: 4 slots below the
+    # top level with stored C, 5 at the top level, all 6 when C is recomputed.
+    # The ops such a launch executes (0-11 only when recomputing, 12-23 only
+    # at the top level) and their resolved operands stay inside those slots.
+    assert "const int nslots = Cst == nullptr ? GF_LOCAL_SLOTS : (top ? 5 : 4);" in src
+    rows = tables["c_local_ops"]
+    for top, recompute, limit in ((False, False, 4), (True, False, 5), (False, True, 6), (True, True, 6)):
+        for q, r in enumerate(rows):
+            if (q < 12 and not recompute) or (12 <= q < 24 and not top):
+                continue
+            a_src, b_src, out = r[0], r[4], r[8]
+            srcs = [{14: 8 if recompute else 2, 15: 7 if top else 1}.get(x, x) for x in (a_src, b_src)]
+            for x in srcs:
+                assert x < 3 or x - 3 < limit, (top, recompute, q, r)
+            assert out < limit, (top, recompute, q, r)
+        # the hooks between table entries write slots 0-3, plus 4 (top) and 5 (recompute)
+        assert limit >= 4
 
 
 def test_gaussian_momenta_sigma_scales_the_unit_draws(pkg, monkeypatch):
