@@ -495,10 +495,12 @@ __constant__ DfOp c_local_ops[31] = {
     {14, 0, 0, 1, 3, 0, 0, 1, 3, 1},  // 30: Dp += C^dag Y^dag
 };
 
-// Blocks per SM of the local adjoint below the top level: its slots 0-3
-// (72 KB) let three blocks share an SM; the top level also needs slot 4.
+// Blocks per SM of the local adjoint below the top level. Its slots 0-3
+// (72 KB) would let three blocks share an SM, but at the 168 registers that
+// takes it spills and measured 4.47 ms per 32^4 launch against 4.31 ms with
+// two blocks at 255 registers.
 #ifndef GF_DF_LOCAL_MINB_LOWER
-#define GF_DF_LOCAL_MINB_LOWER 3
+#define GF_DF_LOCAL_MINB_LOWER 2
 #endif
 template <bool TOP>
 __global__ void __launch_bounds__(128, TOP ? GF_MINB_ADJ(dfl) : GF_DF_LOCAL_MINB_LOWER)
