@@ -571,7 +571,8 @@ def run_wilson_mode(args):
 
 def run_scale_mode(args):
     """Memory-bound scale-up: `--lattice` (64) SU(3), 3-level stout rho = 0.1,
-    beta = 6.2, tau = 1, 30 QPQ steps, mixed precision, with the adjoint
+    beta = 6.2, tau = 1, 30 QPQ steps, in the form `--precision` names (mixed
+    by default; dfloat: the form within the Delta H bound), with the adjoint
     storing each level's C (store) or recomputing it (recompute); peak device
     memory of each, trajectories/s, one fp64 trajectory for the Delta H error,
     then the RK3 flow eps = 0.01 to t = 3 recording E(t)."""
@@ -595,8 +596,9 @@ def run_scale_mode(args):
                             recompute=recompute)
         return U, P, drv
 
+    prec = args.precision if args.precision in ("mixed", "dfloat") else "mixed"
     out = {"mode": "scale", "lattice": [L] * 4, "workload": "%d^4, 3-level stout rho=0.1, beta=6.2, tau=1, "
-           "30 QPQ steps, mixed precision" % L,
+           "30 QPQ steps, %s precision" % (L, prec), "precision": prec,
            "memory_note": "device memory after the first trajectory, before any host transfer (the context's "
                           "staging buffer for host transfers, one fp64 link field, is not included)"}
     # the start configuration in the host layout, from a context of its own
@@ -610,7 +612,7 @@ def run_scale_mode(args):
         del Ut
         torch.cuda.synchronize()
     for recompute in ((True,) if args.recompute_only else (False, True)):
-        U, P, drv = setup("mixed", recompute)
+        U, P, drv = setup(prec, recompute)
         pkg.gaussian_momenta_(P, seed=SEED, sweep=0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
