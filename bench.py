@@ -662,8 +662,10 @@ def run_scale_mode(args):
 def run_kernel_mode(args):
     """Small single-family cases for profiler captures: `force` repeats the
     stout force of the workload (update_momenta_; `--levels 0`: the Wilson
-    force on thin links), `link` the link update (update_gaugefields_), both
-    in the form `--precision` names, and `plaquette` the plaquette sum."""
+    force on thin links; `--levels 0 --c-rect c1`: the plaquette + rectangle
+    force of beta (c0 plaq + c1 rect), c0 = 1 - 8 c1, e.g. Iwasaki c1 =
+    -0.331), `link` the link update (update_gaugefields_), both in the form
+    `--precision` names, and `plaquette` the plaquette sum."""
     import torch
     import __graft_entry__ as entry
     pkg = entry.build()
@@ -671,7 +673,9 @@ def run_kernel_mode(args):
     U, P, drv = make_setup(pkg, L, args.precision, SEED)
     if args.levels == 0:
         action = pkg.GaugeAction(U)
-        pkg.push_(action, BETA / 2, "plaquette")
+        pkg.push_(action, (1 - 8 * args.c_rect) * BETA / 2, "plaquette")
+        if args.c_rect != 0.0:
+            pkg.push_(action, args.c_rect * BETA / 2, "rectangular")
         drv = pkg.md_driver(U, action, steps=NSTEPS, trajectory_length=TAU, precision=args.precision)
     pkg.gaussian_momenta_(P, seed=SEED)
     calls = []
@@ -687,7 +691,7 @@ def run_kernel_mode(args):
         U.ctx.sync()
         calls.append(time.perf_counter() - t0)
     print(json.dumps({"mode": args.mode, "precision": args.precision, "lattice": [L] * 4,
-                      "stout_levels": len(RHO) if args.levels is None else args.levels,
+                      "stout_levels": len(RHO) if args.levels is None else args.levels, "c_rect": args.c_rect,
                       "ms_per_call": 1e3 * min(calls[args.warmup:])}))
     return 0
 
@@ -713,6 +717,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--therm", type=int, default=10, help="thermalisation trajectories before the Delta H check")
     ap.add_argument("--levels", type=int, default=None, help="force mode: 0 = Wilson force without smearing")
+    ap.add_argument("--c-rect", type=float, default=0.0,
+                    help="force mode with --levels 0: rectangle coefficient c1 (Iwasaki -0.331)")
     ap.add_argument("--mode", default="hmc", choices=["hmc", "force", "link", "plaquette", "precision", "wilson",
                                                       "scale"],
                     help="hmc: the benchmark; force/link: one kernel family, for profiler captures; "

@@ -112,13 +112,13 @@ SIGNATURES = {
 
 KERNEL_CLASSES = ["plaquette", "force", "link_update", "stout_fwd", "bwd_local", "bwd_gather", "stout_fwd64",
                   "bwd_local64", "bwd_gather64", "other", "link_update_df", "stout_fwd_df", "force_df",
-                  "bwd_local_df", "bwd_gather_df", "rect"]
+                  "bwd_local_df", "bwd_gather_df", "rect", "rect_df"]
 # arithmetic precision of each class (the force class follows its links)
 KERNEL_PRECISION = {"plaquette": "fp64", "force": "fp32", "link_update": "fp64", "stout_fwd": "fp32",
                     "bwd_local": "fp32", "bwd_gather": "fp32", "stout_fwd64": "fp64", "bwd_local64": "fp64",
                     "bwd_gather64": "fp64", "other": "fp64", "link_update_df": "df", "stout_fwd_df": "df",
                     "force_df": "df", "bwd_local_df": "df", "bwd_gather_df": "df",
-                    "rect": "fp64"}
+                    "rect": "fp64", "rect_df": "df"}
 
 _lib = None
 

@@ -456,8 +456,8 @@ class OmelyanPQP:
 class MDActionSet:
     """MDActionSet(; name=action, ...) (molecular_dynamics.jl:45-66): named
     action providers whose potentials and forces add. On this backend the
-    members are GaugeActions of plaquette (and, in the plain fp64 form on thin
-    links, rectangle) loops on the driver's links. Their forces are linear in
+    members are GaugeActions of plaquette and rectangle loops on the driver's
+    (smeared) links. Their forces are linear in
     the loop coefficients, so the force of any group of members is the force
     of one action with the group's summed coefficients: a group's momentum
     update is one fused force pass."""
@@ -632,9 +632,6 @@ def md_driver(U, action, steps, trajectory_length=1.0, integrator=None, smearing
     if not (isinstance(action, MDActionSet) or (isinstance(action, GaugeAction) and action.terms)):
         raise ValueError("md_action_workspace is not implemented for %s" % type(action).__name__)
     _validate_integrator(integrator, action)
-    if action.c_rect != 0.0 and (precision != "fp64" or smearing is not None):
-        raise ValueError("the rectangle loops run in the plain fp64 form on thin links (precision 'fp64', "
-                         "no smearing)")
     return MDDriver(action, integrator, float(trajectory_length), int(steps), smearing, precision, reunitarize,
                     recompute)
 

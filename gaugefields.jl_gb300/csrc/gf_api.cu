@@ -139,6 +139,7 @@ extern "C" int gf_ctx_destroy(gf_ctx* ctx) {
   field_delete(ctx->w_link64b);
   for (int i = 0; i < 4; ++i) field_delete(ctx->w_mom[i]);
   field_delete(ctx->w_link32);
+  field_delete(ctx->w_linkdf);
   if (ctx->w_stout64) gf_stout_destroy(ctx->w_stout64);
   if (ctx->w_stout32) gf_stout_destroy(ctx->w_stout32);
   if (ctx->w_stoutdf) gf_stout_destroy(ctx->w_stoutdf);
@@ -533,8 +534,6 @@ static void check_md(const gf_md_params* p) {
   need(p->nstout >= 0 && p->nstout <= GF_MAX_STOUT, "md: nstout must be 0..GF_MAX_STOUT");
   for (int l = 0; l < p->nstout; ++l) need(std::isfinite(p->rho[l]), "md: rho must be finite");
   need(std::isfinite(p->c_rect), "md: c_rect must be finite");
-  need(p->c_rect == 0.0 || (p->precision == GF_FP64 && p->nstout == 0),
-       "md: the rectangle term runs in the plain fp64 form on thin links (precision GF_FP64, nstout 0)");
 }
 
 // The context's stack for a stack precision. The mixed form's Hamiltonian
@@ -568,12 +567,15 @@ static gf_stout* ctx_stout(gf_ctx* ctx, const gf_md_params* p, int precision) {
 #endif
 static double potential(gf_ctx* ctx, const gf_field* U, const gf_md_params* p) {
   bool df = (GF_DF_HAMILTONIAN && p->precision == GF_MIXED) || p->precision == GF_DFLOAT;
-  if (p->nstout == 0 && p->c_rect != 0.0)
-    return -(p->beta / 3.0) * plaquette_sum(ctx, U) - (2.0 / 3.0) * p->c_rect * rectangle_sum(ctx, U);
-  if (p->nstout == 0) return -(p->beta / 3.0) * plaquette_sum(ctx, U);
-  gf_stout* st = ctx_stout(ctx, p, df ? GF_PREC_DF : GF_FP64);
-  stout_forward(ctx, st, U, nullptr);
-  return -(p->beta / 3.0) * plaquette_sum(ctx, stout_top(st));
+  const gf_field* links = U;
+  if (p->nstout > 0) {
+    gf_stout* st = ctx_stout(ctx, p, df ? GF_PREC_DF : GF_FP64);
+    stout_forward(ctx, st, U, nullptr);
+    links = stout_top(st);
+  }
+  double v = -(p->beta / 3.0) * plaquette_sum(ctx, links);
+  if (p->c_rect != 0.0) v -= (2.0 / 3.0) * p->c_rect * rectangle_sum(ctx, links);
+  return v;
 }
 
 static double hamiltonian(gf_ctx* ctx, const gf_field* U, const gf_field* P, const gf_md_params* p) {
@@ -586,7 +588,17 @@ static void mom_update(gf_ctx* ctx, gf_field* P, const gf_field* U, const gf_fie
                        const gf_md_params* p) {
   const gf_field* links = (p->precision == GF_MIXED) ? U32 : U;
   if (p->nstout == 0 && p->c_rect != 0.0) {
-    loops_force_coef(ctx, U, P, eps * (-1.0 / 3.0) * (0.5 * p->beta), eps * (-1.0 / 3.0) * p->c_rect, 1.0);
+    loops_force_coef(ctx, links, P, eps * (-1.0 / 3.0) * (0.5 * p->beta), eps * (-1.0 / 3.0) * p->c_rect, 1.0,
+                     p->precision == GF_DFLOAT);
+    return;
+  }
+  if (p->c_rect != 0.0) {
+    // smeared plaquette + rectangle action: dS/dUbar = beta/2 S + c_rect R on
+    // the top level, written into the stack's D[1] and back-propagated
+    gf_stout* st = ctx_stout(ctx, p, p->precision);
+    stout_forward(ctx, st, links, nullptr);
+    loops_dsdu(ctx, stout_top(st), st->D[1], 0.5 * p->beta, p->c_rect);
+    stout_backward(ctx, st, st->D[1], p->beta, nullptr, P, eps);
     return;
   }
   if (p->nstout == 0) {

@@ -69,6 +69,7 @@ struct gf_ctx {
   gf_field* w_link64b;    // W2 of the flow
   gf_field* w_mom[4];     // F0, F1, F2, Ftmp of the RK3 flow (fp64 coefficients)
   gf_field* w_link32;     // fp32 12-real shadow of the thin links (mixed form)
+  gf_field* w_linkdf;     // double-float-native copy of the thin links (double-float rectangle force)
   // Two scratch blocks of one fp64 link field each, shared by the mixed form's
   // internal stacks: the Hamiltonian's double-float level buffers and the
   // force adjoint's Z, Dp, D[0], D[1] (fp32). They are never live together:
@@ -174,7 +175,11 @@ void wilson_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double coef,
 double rectangle_sum(gf_ctx* ctx, const gf_field* U);  // sum_x sum_{mu<nu} Re tr (R1x2 + R2x1)
 // P <- keep * P + TA-coefficients(U_mu (cp S_mu + cr R_mu)), S the six
 // plaquette staples and R the eighteen rectangle staples of U_mu.
-void loops_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double cp, double cr, double keep);
+void loops_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double cp, double cr, double keep,
+                      bool df = false);
+// D = cp S + cr R (plaquette and rectangle staples) on a stack's top level:
+// LINK64 -> MAT64, LINK32 -> MAT32, LINKDF -> MATDF (double-float)
+void loops_dsdu(gf_ctx* ctx, const gf_field* Ubar, gf_field* D, double cp, double cr);
 
 // ---- link update (gf_update.cu) ----
 // U <- exp(i eps P) U, optional re-unitarisation, optional fp32 shadow copy.

@@ -18,6 +18,7 @@
 // c_rect S_rect and F = -(1/3) TA(U_mu dS/dU_mu), as for the Wilson action.
 #include "gf_internal.h"
 #include "stencil.cuh"
+#include "dfslots.cuh"
 
 namespace gf {
 
@@ -39,7 +40,8 @@ __device__ __forceinline__ int site_off(const Geom& g, const Site& st, int mu, i
 
 // Sum over mu < nu of Re tr (R^{1x2}_{mu nu}(x) + R^{2x1}_{mu nu}(x)) at one
 // site, each rectangle as Re tr(A B^+) of its two three-link halves.
-__device__ double rect_site(const SrcRect& U, const Geom& g, const Site& st, int s) {
+template <class SRC>
+__device__ double rect_site(const SRC& U, const Geom& g, const Site& st, int s) {
   const int V = g.vol;
   double v = 0.0;
 #pragma unroll 1
@@ -62,7 +64,8 @@ __device__ double rect_site(const SrcRect& U, const Geom& g, const Site& st, int
   return v;
 }
 
-__global__ void __launch_bounds__(128) k_rect_sum(SrcRect U, Geom g, double* __restrict__ part) {
+template <class SRC>
+__global__ void __launch_bounds__(128) k_rect_sum(SRC U, Geom g, double* __restrict__ part) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   double v = 0.0;
   if (s < g.vol) {
@@ -73,10 +76,11 @@ __global__ void __launch_bounds__(128) k_rect_sum(SrcRect U, Geom g, double* __r
 }
 
 // acc += the six rectangle staples (a)-(f) of U_mu(x) in the mu-nu plane
-__device__ __forceinline__ void add_rect_staples(mat3<double>& acc, const SrcRect& U, const Geom& g, const Site& st,
-                                                 int s, int mu, int nu) {
+template <typename R, class SRC>
+__device__ __forceinline__ void add_rect_staples(mat3<R>& acc, const SRC& U, const Geom& g, const Site& st, int s,
+                                                 int mu, int nu) {
   const int V = g.vol;
-  mat3<double> t;
+  mat3<R> t;
   // (a)
   t = mul_nn(U(nu, site_off(g, st, mu, 1, nu, 0), V), U(nu, site_off(g, st, mu, 1, nu, 1), V));
   t = mul_na(t, U(mu, site_off(g, st, mu, 0, nu, 2), V));
@@ -109,56 +113,232 @@ __device__ __forceinline__ void add_rect_staples(mat3<double>& acc, const SrcRec
   mac_nn(acc, t, U(mu, site_off(g, st, mu, -1, nu, 0), V));
 }
 
+// cp S_mu(x) + cr R_mu(x): S the six plaquette staples, R the eighteen
+// rectangle staples of U_mu(x)
+template <typename R, class SRC>
+__device__ __forceinline__ mat3<R> loops_dsdu(const SRC& U, const Geom& g, const Site& st, int s, int mu, R cp,
+                                              R cr) {
+  mat3<R> S = zero3<R>();
+  mat3<R> Q = zero3<R>();
+#pragma unroll 1
+  for (int k = 1; k < 4; ++k) {
+    const int nu = (mu + k) & 3;
+    add_staple_pair<R>(S, U, g, st, s, mu, nu);
+    add_rect_staples<R>(Q, U, g, st, s, mu, nu);
+  }
+  mat3<R> T = scale(cp, S);
+  axpy_to(T, cr, Q);
+  return T;
+}
+
 // P_mu(x) <- keep * P_mu(x) + c(U_mu(x) (cp S_mu(x) + cr R_mu(x))), c = su(3)
-// coefficients of TA; S the six plaquette staples, R the eighteen rectangle
-// staples (keep = 0 overwrites without reading P).
-__global__ void __launch_bounds__(128) k_force_rect(SrcRect U, double* __restrict__ P, Geom g, double cp, double cr,
-                                                    double keep) {
+// coefficients of TA (keep = 0 overwrites without reading P); arithmetic in
+// R (fp64 on the plain form's links, fp32 on the mixed form's 12-real links)
+template <typename R, class SRC>
+__global__ void __launch_bounds__(128) k_force_rect(SRC U, double* __restrict__ P, Geom g, R cp, R cr, double keep) {
   int s, mu;
   link_of_thread(s, mu);
   if (s >= g.vol) return;
   Site st = site_of(g, s);
   const int V = g.vol;
-  mat3<double> S = zero3<double>();
-  mat3<double> R = zero3<double>();
-#pragma unroll 1
-  for (int k = 1; k < 4; ++k) {
-    const int nu = (mu + k) & 3;
-    add_staple_pair<double>(S, U, g, st, s, mu, nu);
-    add_rect_staples(R, U, g, st, s, mu, nu);
-  }
-  mat3<double> T = scale(cp, S);
-  axpy_to(T, cr, R);
-  mat3<double> M = mul_nn(U(mu, s, V), T);
-  double c[8];
+  const mat3<R> T = loops_dsdu<R>(U, g, st, s, mu, cp, cr);
+  mat3<R> M = mul_nn(U(mu, s, V), T);
+  R c[8];
   ta_coeffs(M, c);
   double* p = P + (size_t)mu * 8 * V + s;
 #pragma unroll
   for (int a = 0; a < 8; ++a) {
     double old = (keep != 0.0) ? keep * p[(size_t)a * V] : 0.0;
-    p[(size_t)a * V] = old + c[a];
+    p[(size_t)a * V] = old + to_f64(c[a]);
   }
 }
 
-double rectangle_sum(gf_ctx* ctx, const gf_field* U) {
-  if (U->kind != GF_LINK64 && U->kind != GF_MAT64) throw gf_error(GF_EINVAL, "rectangle: links must be LINK64");
-  const int V = ctx->geom.vol;
-  const int nb = blocks_for(V, 128);
+// D_mu(x) = cp S_mu(x) + cr R_mu(x): dS/dUbar of the plaquette + rectangle
+// action on the top level of a stout stack (the input of its adjoint)
+template <typename R, class SRC>
+__global__ void __launch_bounds__(128) k_dsdu_rect(SRC U, typename LinkFull<R>::elem* __restrict__ D, Geom g, R cp,
+                                                   R cr) {
+  int s, mu;
+  link_of_thread(s, mu);
+  if (s >= g.vol) return;
+  Site st = site_of(g, s);
+  LinkFull<R>::store(D, mu, s, g.vol, loops_dsdu<R>(U, g, st, s, mu, cp, cr));
+}
+
+// --------------------------------------------------------------------------
+// The same force in double-float arithmetic (the GF_DFLOAT form on thin
+// links), as a loop over a table of products with one inlined fixed-grid
+// product (the double-float stencils overflow the instruction cache when
+// their products are inlined). Per plane (mu, nu): ops 0-3 add the two
+// plaquette staples to S (add_staple_pair), ops 4-27 the six rectangle
+// staples (a)-(f) above to R, four products each. An operand is the link of
+// direction mu or nu at x + mo e_mu + no e_nu (optionally daggered) or the
+// running product t; results go to t, S or R.
+// --------------------------------------------------------------------------
+struct DfOpR {
+  // src 0: link (dir 0 = mu, 1 = nu; offsets mo, no), src 1: slot t
+  signed char a_src, a_dir, a_mo, a_no, a_dag, b_src, b_dir, b_mo, b_no, b_dag, out, accumulate;
+};
+#define GF_RECT_T 0
+#define GF_RECT_S 1
+#define GF_RECT_R 2
+#define GF_RECT_SLOTS 3
+__constant__ DfOpR c_rect_ops[28] = {
+    // plaquette staples: U_nu(x+mu) U_mu(x+nu)^+ U_nu(x)^+ and U_nu(x+mu-nu)^+ U_mu(x-nu)^+ U_nu(x-nu)
+    {0, 1, 1, 0, 0, 0, 0, 0, 1, 1, 0, 0}, {1, 0, 0, 0, 0, 0, 1, 0, 0, 1, 1, 1},
+    {0, 1, 1, -1, 1, 0, 0, 0, -1, 1, 0, 0}, {1, 0, 0, 0, 0, 0, 1, 0, -1, 0, 1, 1},
+    // (a) U_nu(x+mu) U_nu(x+mu+nu) U_mu(x+2nu)^+ U_nu(x+nu)^+ U_nu(x)^+
+    {0, 1, 1, 0, 0, 0, 1, 1, 1, 0, 0, 0}, {1, 0, 0, 0, 0, 0, 0, 0, 2, 1, 0, 0},
+    {1, 0, 0, 0, 0, 0, 1, 0, 1, 1, 0, 0}, {1, 0, 0, 0, 0, 0, 1, 0, 0, 1, 2, 1},
+    // (b) U_nu(x+mu-nu)^+ U_nu(x+mu-2nu)^+ U_mu(x-2nu)^+ U_nu(x-2nu) U_nu(x-nu)
+    {0, 1, 1, -1, 1, 0, 1, 1, -2, 1, 0, 0}, {1, 0, 0, 0, 0, 0, 0, 0, -2, 1, 0, 0},
+    {1, 0, 0, 0, 0, 0, 1, 0, -2, 0, 0, 0}, {1, 0, 0, 0, 0, 0, 1, 0, -1, 0, 2, 1},
+    // (c) U_mu(x+mu) U_nu(x+2mu) U_mu(x+mu+nu)^+ U_mu(x+nu)^+ U_nu(x)^+
+    {0, 0, 1, 0, 0, 0, 1, 2, 0, 0, 0, 0}, {1, 0, 0, 0, 0, 0, 0, 1, 1, 1, 0, 0},
+    {1, 0, 0, 0, 0, 0, 0, 0, 1, 1, 0, 0}, {1, 0, 0, 0, 0, 0, 1, 0, 0, 1, 2, 1},
+    // (d) U_mu(x+mu) U_nu(x+2mu-nu)^+ U_mu(x+mu-nu)^+ U_mu(x-nu)^+ U_nu(x-nu)
+    {0, 0, 1, 0, 0, 0, 1, 2, -1, 1, 0, 0}, {1, 0, 0, 0, 0, 0, 0, 1, -1, 1, 0, 0},
+    {1, 0, 0, 0, 0, 0, 0, 0, -1, 1, 0, 0}, {1, 0, 0, 0, 0, 0, 1, 0, -1, 0, 2, 1},
+    // (e) U_nu(x+mu) U_mu(x+nu)^+ U_mu(x-mu+nu)^+ U_nu(x-mu)^+ U_mu(x-mu)
+    {0, 1, 1, 0, 0, 0, 0, 0, 1, 1, 0, 0}, {1, 0, 0, 0, 0, 0, 0, -1, 1, 1, 0, 0},
+    {1, 0, 0, 0, 0, 0, 1, -1, 0, 1, 0, 0}, {1, 0, 0, 0, 0, 0, 0, -1, 0, 0, 2, 1},
+    // (f) U_nu(x+mu-nu)^+ U_mu(x-nu)^+ U_mu(x-mu-nu)^+ U_nu(x-mu-nu) U_mu(x-mu)
+    {0, 1, 1, -1, 1, 0, 0, 0, -1, 1, 0, 0}, {1, 0, 0, 0, 0, 0, 0, -1, -1, 1, 0, 0},
+    {1, 0, 0, 0, 0, 0, 1, -1, -1, 0, 0, 0}, {1, 0, 0, 0, 0, 0, 0, -1, 0, 0, 2, 1},
+};
+
+__device__ __forceinline__ mat3<dfl> rect_operand(int src, int dir, int mo, int no, int dagger, const float* sm, int tid,
+                                                  const float4* __restrict__ U, const Geom& g, const Site& st, int mu,
+                                                  int nu) {
+  mat3<dfl> m;
+  if (src == 1) m = slot_load(sm, GF_RECT_T, tid);
+  else m = LinkDfn::load(U, dir ? nu : mu, site_off(g, st, mu, mo, nu, no), g.vol);
+  if (dagger) m = dag(m);
+  return m;
+}
+
+// P_mu(x) <- keep * P_mu(x) + c(U_mu(x) (cp S_mu(x) + cr R_mu(x))) as
+// k_force_rect, the staples, the combination and the projection in
+// double-float, on double-float-native links; DSDU: D_mu(x) = cp S + cr R
+// (as k_dsdu_rect, double-float-native) instead
+template <bool DSDU>
+__global__ void __launch_bounds__(128, 3)
+    k_force_rect_df(const float4* __restrict__ U, double* __restrict__ P, float4* __restrict__ D, Geom g, dfl cp,
+                    dfl cr, double keep) {
+  extern __shared__ __align__(16) float sm[];  // GF_RECT_SLOTS slots of 36 x 128 floats
+  const int tid = threadIdx.x;
+  int s, mu;
+  link_of_thread(s, mu);
+  if (s >= g.vol) return;  // the slots are per thread: no block-wide synchronisation
+  const Site st = site_of(g, s);
+  slot_store(sm, GF_RECT_S, tid, zero3<dfl>());
+  slot_store(sm, GF_RECT_R, tid, zero3<dfl>());
+#pragma unroll 1
+  for (int k = 1; k < 4; ++k) {
+    const int nu = (mu + k) & 3;
+#pragma unroll 1
+    for (int q = 0; q < 28; ++q) {
+      const DfOpR op = c_rect_ops[q];
+      const mat3<dfl> A = rect_operand(op.a_src, op.a_dir, op.a_mo, op.a_no, op.a_dag, sm, tid, U, g, st, mu, nu);
+      const mat3<dfl> B = rect_operand(op.b_src, op.b_dir, op.b_mo, op.b_no, op.b_dag, sm, tid, U, g, st, mu, nu);
+      const mat3<dfl> C = op.accumulate ? slot_load(sm, op.out, tid) : zero3<dfl>();
+      slot_store(sm, op.out, tid, dfg_matmul<false, false, true>(A, B, &C));
+    }
+  }
+  const mat3<dfl> S = slot_load(sm, GF_RECT_S, tid), R = slot_load(sm, GF_RECT_R, tid);
+  mat3<dfl> T;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      dfg_cacc a = dfg_cbegin(fabsf(cp.hi) * cabs1(S.e[i][j]) + fabsf(cr.hi) * cabs1(R.e[i][j]));
+      dfg_rcterm(a, cp, S.e[i][j]);
+      dfg_rcterm(a, cr, R.e[i][j]);
+      T.e[i][j] = dfg_cend(a);
+    }
+  if (DSDU) {
+    LinkDfn::store(D, mu, s, g.vol, T);
+    return;
+  }
+  const mat3<dfl> M = dfg_matmul<false, false, false>(LinkDfn::load(U, mu, s, g.vol), T, nullptr);
+  dfl c[8];
+  ta_coeffs(M, c);
+  double* p = P + (size_t)mu * 8 * g.vol + s;
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    const double old = (keep != 0.0) ? keep * p[(size_t)a * g.vol] : 0.0;
+    p[(size_t)a * g.vol] = old + to_f64(c[a]);
+  }
+}
+
+static void rect_df(gf_ctx* ctx, const float4* U, gf_field* P, gf_field* D, double cp, double cr, double keep) {
+  const size_t smem = (size_t)GF_RECT_SLOTS * 36 * 128 * sizeof(float);
+  auto kern = D ? k_force_rect_df<true> : k_force_rect_df<false>;
+  GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid = stencil_grid(ctx->geom.vol, 128);
+  ProfScope prof(ctx, GF_K_RECT_DF);
+  kern<<<grid, 128, smem, ctx->stream>>>(U, P ? (double*)P->ptr : nullptr, D ? (float4*)D->ptr : nullptr, ctx->geom,
+                                         dfl(cp), dfl(cr), keep);
+  GF_CHECK_LAUNCH();
+}
+
+template <class SRC>
+static double rect_sum_of(gf_ctx* ctx, SRC src) {
+  const int nb = blocks_for(ctx->geom.vol, 128);
   ProfScope prof(ctx, GF_K_RECT);
-  SrcRect src{(const double2*)U->ptr};
   k_rect_sum<<<nb, 128, 0, ctx->stream>>>(src, ctx->geom, ctx->d_partials);
   GF_CHECK_LAUNCH();
   return finish_reduction(ctx, nb);
 }
 
-void loops_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double cp, double cr, double keep) {
+double rectangle_sum(gf_ctx* ctx, const gf_field* U) {
+  if (U->kind == GF_LINK64 || U->kind == GF_MAT64) return rect_sum_of(ctx, SrcRect{(const double2*)U->ptr});
+  // top level of a double-float stack: fp64 arithmetic on hi + lo
+  if (U->kind == GF_LINKDF) return rect_sum_of(ctx, LinkSrcDfn64{(const float4*)U->ptr});
+  throw gf_error(GF_EINVAL, "rectangle: links must be LINK64");
+}
+
+void loops_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double cp, double cr, double keep, bool df) {
   if (P->kind != GF_MOM64) throw gf_error(GF_EINVAL, "force: output must be MOM64");
-  if (U->kind != GF_LINK64 && U->kind != GF_MAT64)
-    throw gf_error(GF_EINVAL, "force: the rectangle force takes LINK64 links");
   dim3 grid = stencil_grid(ctx->geom.vol, 128);
+  if (df) {
+    if (U->kind != GF_LINK64) throw gf_error(GF_EINVAL, "force: the double-float rectangle force takes LINK64 links");
+    // a double-float-native copy of the links, converted once per force
+    if (!ctx->w_linkdf) ctx->w_linkdf = field_new(ctx, GF_LINKDF);
+    copy_field(ctx, ctx->w_linkdf, U);
+    rect_df(ctx, (const float4*)ctx->w_linkdf->ptr, P, nullptr, cp, cr, keep);
+    return;
+  }
+  if (U->kind == GF_LINK64 || U->kind == GF_MAT64) {
+    ProfScope prof(ctx, GF_K_RECT);
+    k_force_rect<double><<<grid, 128, 0, ctx->stream>>>(SrcRect{(const double2*)U->ptr}, (double*)P->ptr, ctx->geom,
+                                                        cp, cr, keep);
+  } else if (U->kind == GF_LINK32) {
+    ProfScope prof(ctx, GF_K_RECT);
+    k_force_rect<float><<<grid, 128, 0, ctx->stream>>>(LinkSrc<float, true>{(const float4*)U->ptr}, (double*)P->ptr,
+                                                       ctx->geom, (float)cp, (float)cr, keep);
+  } else {
+    throw gf_error(GF_EINVAL, "force: the rectangle force takes LINK64 or LINK32 links");
+  }
+  GF_CHECK_LAUNCH();
+}
+
+void loops_dsdu(gf_ctx* ctx, const gf_field* Ubar, gf_field* D, double cp, double cr) {
+  dim3 grid = stencil_grid(ctx->geom.vol, 128);
+  if (Ubar->kind == GF_LINKDF && D->kind == GF_MATDF) {
+    rect_df(ctx, (const float4*)Ubar->ptr, nullptr, D, cp, cr, 0.0);
+    return;
+  }
   ProfScope prof(ctx, GF_K_RECT);
-  SrcRect src{(const double2*)U->ptr};
-  k_force_rect<<<grid, 128, 0, ctx->stream>>>(src, (double*)P->ptr, ctx->geom, cp, cr, keep);
+  if (Ubar->kind == GF_LINK64 && D->kind == GF_MAT64) {
+    k_dsdu_rect<double><<<grid, 128, 0, ctx->stream>>>(SrcRect{(const double2*)Ubar->ptr}, (double2*)D->ptr,
+                                                       ctx->geom, cp, cr);
+  } else if (Ubar->kind == GF_LINK32 && D->kind == GF_MAT32) {
+    k_dsdu_rect<float><<<grid, 128, 0, ctx->stream>>>(LinkSrc<float, true>{(const float4*)Ubar->ptr},
+                                                      (float2*)D->ptr, ctx->geom, (float)cp, (float)cr);
+  } else {
+    throw gf_error(GF_EINVAL, "loops dS/dU: link and matrix kinds do not match");
+  }
   GF_CHECK_LAUNCH();
 }
 

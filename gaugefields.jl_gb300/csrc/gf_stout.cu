@@ -20,6 +20,7 @@
 // and momentum update at the bottom level).
 #include "gf_internal.h"
 #include "stencil.cuh"
+#include "dfslots.cuh"
 #include <type_traits>
 
 
@@ -244,28 +245,6 @@ struct DfOp {
   // direction, 1 the loop axis; site: index into the kernel's five sites
   unsigned char a_src, a_dir, a_site, a_dag, b_src, b_dir, b_site, b_dag, out, accumulate;
 };
-
-// slot `slot` of this thread: 9 float4 (one per complex element),
-// element-major, so a warp's 128-bit accesses cover consecutive banks
-// (blocks of 128 threads; 36 floats per thread and slot)
-__device__ __forceinline__ mat3<dfl> slot_load(const float* sm, int slot, int tid) {
-  mat3<dfl> m;
-  const float4* q = reinterpret_cast<const float4*>(sm) + slot * 9 * 128 + tid;
-#pragma unroll
-  for (int e = 0; e < 9; ++e) {
-    const float4 v = q[e * 128];
-    m.e[e / 3][e % 3] = mk(dfl(v.x, v.y), dfl(v.z, v.w));
-  }
-  return m;
-}
-__device__ __forceinline__ void slot_store(float* sm, int slot, int tid, const mat3<dfl>& m) {
-  float4* q = reinterpret_cast<float4*>(sm) + slot * 9 * 128 + tid;
-#pragma unroll
-  for (int e = 0; e < 9; ++e) {
-    const cplx<dfl> v = m.e[e / 3][e % 3];
-    q[e * 128] = make_float4(v.re.hi, v.re.lo, v.im.hi, v.im.lo);
-  }
-}
 
 struct DfSites {
   int x[5];
@@ -699,14 +678,15 @@ const gf_field* stout_top(const gf_stout* st) { return st->lev_in[st->nlev]; }
 
 // Double-float adjoint on native storage. A caller's dS/dUbar (fp64) is
 // converted into D[1] first: the top level's local kernel reads it before
-// that level's gather overwrites D[1]. A caller's dS/dU receives the bottom
+// that level's gather overwrites D[1] (an internal caller may have written it
+// there, double-float-native, already). A caller's dS/dU receives the bottom
 // gather's output in fp64.
 static void backward_df(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, double beta, gf_field* dSdU,
                         gf_field* P, double eps, double* dsdrho) {
   dim3 grid = stencil_grid(ctx->geom.vol, 128);
   const float4* dbar = nullptr;
   if (dSdUbar) {
-    copy_field(ctx, st->D[1], dSdUbar);
+    if (dSdUbar != st->D[1]) copy_field(ctx, st->D[1], dSdUbar);
     dbar = (const float4*)st->D[1]->ptr;
   }
   int cur = 0;
@@ -795,7 +775,8 @@ void stout_backward(gf_ctx* ctx, gf_stout* st, const gf_field* dSdUbar, double b
   if (st->fwd_only) throw gf_error(GF_EINVAL, "stout backward: forward-only stack");
   if (st->nlev < 1) throw gf_error(GF_EINVAL, "stout backward needs at least one level");
   int mk = st->precision == GF_MIXED ? GF_MAT32 : GF_MAT64;
-  if (dSdUbar && dSdUbar->kind != mk) throw gf_error(GF_EINVAL, "stout backward: dS/dUbar kind does not match the stack precision");
+  // a dS/dUbar in the stack's own D[1] (written there by the caller) is read in place
+  if (dSdUbar && dSdUbar != st->D[1] && dSdUbar->kind != mk) throw gf_error(GF_EINVAL, "stout backward: dS/dUbar kind does not match the stack precision");
   // dSdU == NULL without P: only dS/drho is wanted (the thin-link result stays internal)
   if (!P && dSdU && dSdU->kind != mk) throw gf_error(GF_EINVAL, "stout backward: dS/dU kind does not match the stack precision");
   if (!P && !dSdU && !dsdrho) throw gf_error(GF_EINVAL, "stout backward: no output");

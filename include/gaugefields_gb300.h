@@ -85,8 +85,10 @@ typedef struct gf_md_params {
   double c_rect;         /* coefficient of the rectangle loops,
                             push!(action, c_rect, rect U rect') (make_rect,
                             src/autostaples/wilsonloops.jl:304-330); 0 for the
-                            plain Wilson action. Nonzero needs precision
-                            GF_FP64 and nstout 0 (thin links). */
+                            plain Wilson action. Every precision form; with
+                            stout levels the loops are those of the smeared
+                            links (dS/dUbar = beta/2 S + c_rect R on the top
+                            level, back-propagated by the stout adjoint). */
 } gf_md_params;
 
 /* ---- context ------------------------------------------------------------ */
@@ -286,7 +288,8 @@ int gf_plaquette_noalloc(const void* links, const int L[4], double* out, void* s
 #define GF_K_BWD_LOCAL_DF 13    /* stout adjoint, local part, double-float */
 #define GF_K_BWD_GATHER_DF 14   /* stout adjoint, gather (+ force), double-float */
 #define GF_K_RECT 15            /* rectangle loop sum and plaquette + rectangle force (fp64) */
-#define GF_K_COUNT 16
+#define GF_K_RECT_DF 16         /* plaquette + rectangle force in double-float */
+#define GF_K_COUNT 17
 /* Enable (on != 0) or disable CUDA-event timing of every kernel launch on the
  * context's stream; enabling clears the accumulators. */
 int gf_prof_enable(gf_ctx* ctx, int on);

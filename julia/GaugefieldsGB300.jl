@@ -323,9 +323,10 @@ function loop_coefficients(action::Gaugefields.GaugeAction)
 end
 
 """
-    StoutWilsonAction_GB300(beta, rho; precision=GF_DFLOAT, recompute=false)
+    StoutWilsonAction_GB300(beta, rho; precision=GF_DFLOAT, recompute=false, c_rect=0.0)
 
 An MD action provider: the Wilson action `push!(action, beta/2, plaq ∪ plaq')`
+(with `c_rect` ≠ 0 also `push!(action, c_rect, rect ∪ rect')`, e.g. Iwasaki)
 evaluated on `length(rho)` plaquette stout levels of the thin links. The
 force runs the hand-written stout adjoint on the device. `precision` selects
 the plain fp64 form (`GF_FP64`), the double-float form (`GF_DFLOAT`, Delta H
@@ -336,12 +337,15 @@ struct StoutWilsonAction_GB300
     rho::Vector{Float64}
     precision::Int
     recompute::Bool
+    c_rect::Float64
 end
-function StoutWilsonAction_GB300(beta::Real, rho; precision::Integer=GF_DFLOAT, recompute::Bool=false)
+function StoutWilsonAction_GB300(beta::Real, rho; precision::Integer=GF_DFLOAT, recompute::Bool=false,
+                                 c_rect::Real=0.0)
     r = collect(Float64, rho)
     1 <= length(r) <= GF_MAX_STOUT || throw(ArgumentError("1..$GF_MAX_STOUT stout levels are supported"))
     precision in (GF_FP64, GF_MIXED, GF_DFLOAT) || throw(ArgumentError("precision must be GF_FP64, GF_MIXED or GF_DFLOAT"))
-    return StoutWilsonAction_GB300(Float64(beta), r, Int(precision), recompute)
+    isfinite(c_rect) || throw(ArgumentError("c_rect must be finite"))
+    return StoutWilsonAction_GB300(Float64(beta), r, Int(precision), recompute, Float64(c_rect))
 end
 
 # The workspace of every GB300 provider: the gf_md_params of its action and
@@ -358,7 +362,7 @@ end
 function action_params(action::StoutWilsonAction_GB300)
     rho = ntuple(i -> i <= length(action.rho) ? action.rho[i] : 0.0, 4)
     return GB300MDParams(action.beta, 1.0, 1, GF_QPQ, action.precision, length(action.rho), rho, 1,
-                         action.recompute ? 1 : 0, 0.0, 0.0)
+                         action.recompute ? 1 : 0, 0.0, action.c_rect)
 end
 
 md_action_workspace(action::Gaugefields.GaugeAction, U::GB300Config) =

@@ -759,9 +759,43 @@ double or_action_loops(const int L[4], const cdbl* U, double c_plaq, double c_re
   return -v / 3.0;
 }
 
-/* F_mu (+)= factor * TA-coefficients of U_mu dS/dU_mu with dS/dU_mu = sum over
- * the sets of c * (staples of U_mu) (calc_dSdUμ!, src/action/GaugeActions.jl:
- * 95-123); accumulate = 0 overwrites F. */
+/* dS/dU_mu(x) = sum over the sets of c * (staples of U_mu) (calc_dSdUμ!,
+ * src/action/GaugeActions.jl:95-123): stp/srp hold the plaquette and
+ * rectangle staples of direction mu */
+static M3 loops_dsdu_at(const Lat* lat, const cdbl* U, const Path* sp, int nsp, const Path* sr, int nsr,
+                        double c_plaq, double c_rect, long x) {
+  M3 acc = mzero();
+  for (int k = 0; k < nsp; ++k) {
+    M3 t = eval_links(U, lat, &sp[k], 0, sp[k].n, x);
+    madd(&acc, c_plaq, &t);
+  }
+  if (c_rect != 0.0)
+    for (int k = 0; k < nsr; ++k) {
+      M3 t = eval_links(U, lat, &sr[k], 0, sr[k].n, x);
+      madd(&acc, c_rect, &t);
+    }
+  return acc;
+}
+
+/* D_mu(x) = dS/dU_mu(x) of every link, in the links' layout (the dS/dUbar
+ * input of the stout adjoint for an action with rectangles) */
+static void loops_dsdu(const Lat* lat, const cdbl* U, double c_plaq, double c_rect, cdbl* D) {
+  Loop lp[12], lr[24];
+  int np = loop_set(0, lp), nr = loop_set(1, lr);
+  for (int mu = 0; mu < 4; ++mu) {
+    Path sp[8], sr[32];
+    int nsp = loop_staples(mu, lp, np, sp);
+    int nsr = loop_staples(mu, lr, nr, sr);
+#pragma omp parallel for schedule(static)
+    for (long x = 0; x < lat->V; ++x) {
+      M3 acc = loops_dsdu_at(lat, U, sp, nsp, sr, nsr, c_plaq, c_rect, x);
+      stm(D, lat, mu, x, &acc);
+    }
+  }
+}
+
+/* F_mu (+)= factor * TA-coefficients of U_mu dS/dU_mu; accumulate = 0
+ * overwrites F. */
 static void loops_force(const int L[4], const cdbl* U, double c_plaq, double c_rect, double factor, int accumulate,
                         double* F) {
   Lat lat = mklat(L);
@@ -773,16 +807,7 @@ static void loops_force(const int L[4], const cdbl* U, double c_plaq, double c_r
     int nsr = loop_staples(mu, lr, nr, sr);
 #pragma omp parallel for schedule(static)
     for (long x = 0; x < lat.V; ++x) {
-      M3 acc = mzero();
-      for (int k = 0; k < nsp; ++k) {
-        M3 t = eval_links(U, &lat, &sp[k], 0, sp[k].n, x);
-        madd(&acc, c_plaq, &t);
-      }
-      if (c_rect != 0.0)
-        for (int k = 0; k < nsr; ++k) {
-          M3 t = eval_links(U, &lat, &sr[k], 0, sr[k].n, x);
-          madd(&acc, c_rect, &t);
-        }
+      M3 acc = loops_dsdu_at(&lat, U, sp, nsp, sr, nsr, c_plaq, c_rect, x);
       M3 u = ld(U, &lat, mu, x);
       M3 w = mmul(&u, &acc);
       double* f = F + ((size_t)mu * lat.V + x) * 8;
@@ -1084,19 +1109,63 @@ double or_stout_action(const int L[4], const cdbl* U, int nlev, const double* rh
 static double g_c_rect = 0.0;
 void or_set_rect(double c_rect) { g_c_rect = c_rect; }
 
+/* Force of the plaquette + rectangle action on stout-smeared links: the
+ * action's dS/dUbar on the top level (loops_dsdu), back-propagated by the
+ * stout adjoint, F = -(1/3) TA(U dS/dU) (the smeared-action force of
+ * src/molecular_dynamics.jl:539-551 with a loop-set action) */
+void or_stout_force_loops(const int L[4], const cdbl* U, int nlev, const double* rho, double c_plaq, double c_rect,
+                          double* F) {
+  if (nlev == 0) {
+    or_force_loops(L, U, c_plaq, c_rect, F);
+    return;
+  }
+  Lat lat = mklat(L);
+  size_t n = (size_t)36 * lat.V;
+  cdbl* Ub = (cdbl*)malloc(sizeof(cdbl) * n);
+  cdbl* dbar = (cdbl*)malloc(sizeof(cdbl) * n);
+  cdbl* dthin = (cdbl*)malloc(sizeof(cdbl) * n);
+  or_stout_forward(L, U, nlev, rho, Ub);
+  loops_dsdu(&lat, Ub, c_plaq, c_rect, dbar);
+  or_stout_backward(L, U, nlev, rho, dbar, dthin, NULL);
+#pragma omp parallel for schedule(static)
+  for (long x = 0; x < lat.V; ++x)
+    for (int mu = 0; mu < 4; ++mu) {
+      M3 u = ld(U, &lat, mu, x);
+      M3 d = ld(dthin, &lat, mu, x);
+      M3 w = mmul(&u, &d);
+      double* f = F + ((size_t)mu * lat.V + x) * 8;
+      for (int a = 0; a < 8; ++a) f[a] = 0;
+      ta_add(f, -1.0 / 3.0, &w);
+    }
+  free(Ub);
+  free(dbar);
+  free(dthin);
+}
+
+double or_stout_action_loops(const int L[4], const cdbl* U, int nlev, const double* rho, double c_plaq,
+                             double c_rect) {
+  if (nlev == 0) return or_action_loops(L, U, c_plaq, c_rect);
+  Lat lat = mklat(L);
+  cdbl* Ub = (cdbl*)malloc(sizeof(cdbl) * (size_t)36 * lat.V);
+  or_stout_forward(L, U, nlev, rho, Ub);
+  double v = or_action_loops(L, Ub, c_plaq, c_rect);
+  free(Ub);
+  return v;
+}
+
 static void mom_update(const int L[4], double* P, const cdbl* U, double eps, double beta, int nstout, const double* rho,
                        double* F) {
   Lat lat = mklat(L);
-  if (nstout == 0 && g_c_rect != 0.0)
-    or_force_loops(L, U, 0.5 * beta, g_c_rect, F);
+  if (g_c_rect != 0.0)
+    or_stout_force_loops(L, U, nstout, rho, 0.5 * beta, g_c_rect, F);
   else
     or_stout_force(L, U, nstout, rho, beta, F);
   mom_axpy(&lat, P, eps, F);
 }
 
 double or_hamiltonian(const int L[4], const cdbl* U, const double* P, double beta, int nstout, const double* rho) {
-  double v = (nstout == 0 && g_c_rect != 0.0) ? or_action_loops(L, U, 0.5 * beta, g_c_rect)
-                                              : or_stout_action(L, U, nstout, rho, beta);
+  double v = (g_c_rect != 0.0) ? or_stout_action_loops(L, U, nstout, rho, 0.5 * beta, g_c_rect)
+                               : or_stout_action(L, U, nstout, rho, beta);
   return v + or_kinetic(L, P) / 2;
 }
 

@@ -80,6 +80,8 @@ def _declare(l):
         "or_loop_trace": ([_P, _P, _I], _D),
         "or_action_loops": ([_P, _P, _D, _D], _D),
         "or_force_loops": ([_P, _P, _D, _D, _P], None),
+        "or_stout_force_loops": ([_P, _P, _I, _P, _D, _D, _P], None),
+        "or_stout_action_loops": ([_P, _P, _I, _P, _D, _D], _D),
         "or_loop_staple_count": ([_I, _I], _I),
         "or_set_rect": ([_D], None),
         "or_flow_loops": ([_P, _P, _D, _I, _D, _D], None),
@@ -285,6 +287,22 @@ def force_loops(L, U, c_plaq, c_rect):
     return F
 
 
+def stout_force_loops(L, U, rho, c_plaq, c_rect):
+    """Force of the plaquette + rectangle action on the stout-smeared links,
+    back-propagated to the thin links."""
+    _chk(U, np.complex128)
+    F = new_mom(L)
+    r = _rho(rho)
+    lib().or_stout_force_loops(_ptr(_L(L)), _ptr(U), len(rho), _ptr(r), float(c_plaq), float(c_rect), _ptr(F))
+    return F
+
+
+def stout_action_loops(L, U, rho, c_plaq, c_rect):
+    _chk(U, np.complex128)
+    r = _rho(rho)
+    return lib().or_stout_action_loops(_ptr(_L(L)), _ptr(U), len(rho), _ptr(r), float(c_plaq), float(c_rect))
+
+
 def flow_loops(L, U, eps, nsteps, c_plaq, c_rect):
     """Gradientflow_general with the plaquette and rectangle loops, in place."""
     _chk(U, np.complex128)
@@ -297,7 +315,8 @@ def loop_staple_count(kind, mu):
 
 def md_trajectory(L, U, P, beta, tau, steps, integrator="QPQ", rho=(), lam=0.1931833275037836, c_rect=0.0):
     """In place on U, P. Returns (H0, H1, dH). integrator: QPQ, PQP or OMELYAN.
-    c_rect: coefficient of the rectangle loops (thin links only)."""
+    c_rect: coefficient of the rectangle loops (of the smeared links when rho
+    is given)."""
     _chk(U, np.complex128)
     _chk(P, np.float64)
     out = np.zeros(3)

@@ -58,7 +58,7 @@ def _fake_library(oracle, log):
             _, P, U, eps, prm = args
             p = prm._obj
             if p.c_rect != 0.0:
-                F = oracle.force_loops(list(P.L), U.U, 0.5 * p.beta, p.c_rect)
+                F = oracle.stout_force_loops(list(P.L), U.U, rho_of(p), 0.5 * p.beta, p.c_rect)
             else:
                 F = oracle.stout_force(list(P.L), U.U, rho_of(p), p.beta)
             P.P += eps.value * F

@@ -8,7 +8,8 @@ make_staple (each forward occurrence of U_mu contributes the rest of its
 loop); the CPU tests pin that rule on the plaquettes against the oracle's own
 Wilson force, and the rectangle force against finite differences of the
 rectangle potential. The GPU tests compare the fused fp64 kernels of
-gf_rect.cu with the oracle."""
+gf_rect.cu with the oracle, and the double-float force (the GF_DFLOAT form)
+with the oracle and with the plain form's trajectories."""
 import numpy as np
 import pytest
 from scipy.linalg import expm
@@ -55,6 +56,37 @@ def test_rectangle_force_is_minus_gradient_of_potential(oracle, coefs):
         assert (vp - vm) / (2 * h) == pytest.approx(-F[mu, x, a], rel=1e-6, abs=1e-7)
 
 
+def test_smeared_rectangle_force_is_minus_gradient_of_the_smeared_potential(oracle):
+    """Two stout levels (rho = 0.1) under the plaquette + rectangle action:
+    the loop-set dS/dUbar on the top level, back-propagated by the stout
+    adjoint, is minus the gradient of the smeared action (central
+    differences); with c_rect = 0 it is the smeared Wilson force."""
+    U = oracle.hot_start(list(L4), 8)
+    rho = (0.1, 0.1)
+    F0 = oracle.stout_force_loops(list(L4), U, rho, 2.85, 0.0)
+    assert np.abs(F0 - oracle.stout_force(list(L4), U, rho, 5.7)).max() < 1e-13
+    assert oracle.stout_action_loops(list(L4), U, rho, 2.85, 0.0) == pytest.approx(
+        oracle.stout_action(list(L4), U, rho, 5.7), rel=1e-14)
+    F = oracle.stout_force_loops(list(L4), U, rho, CP, CR)
+    rng = np.random.RandomState(6)
+    h = 1e-4
+    for _ in range(6):
+        mu, x, a = rng.randint(4), rng.randint(256), rng.randint(8)
+        vp = oracle.stout_action_loops(list(L4), _bump(oracle, U, mu, x, a, h), rho, CP, CR)
+        vm = oracle.stout_action_loops(list(L4), _bump(oracle, U, mu, x, a, -h), rho, CP, CR)
+        assert (vp - vm) / (2 * h) == pytest.approx(-F[mu, x, a], rel=1e-6, abs=1e-7)
+
+
+def test_smeared_iwasaki_md_is_reversible(oracle):
+    U0, P0 = oracle.hot_start(list(L4), 1235), oracle.gauss_mom(list(L4), 98)
+    U, P = U0.copy(), P0.copy()
+    h = oracle.md_trajectory(list(L4), U, P, B_IWA * C0, 0.3, 6, "QPQ", rho=(0.1,), c_rect=CR)
+    oracle.md_trajectory(list(L4), U, P, B_IWA * C0, -0.3, 6, "QPQ", rho=(0.1,), c_rect=CR)
+    assert np.abs(U - U0).max() < 2e-12 and np.abs(P - P0).max() < 2e-12
+    assert h[0] == pytest.approx(oracle.stout_action_loops(list(L4), U0, (0.1,), CP, CR)
+                                 + oracle.kinetic(list(L4), P0) / 2, rel=1e-14)
+
+
 def test_rectangle_sum_is_gauge_invariant(oracle):
     from test_oracle import oracle_shift
     U = oracle.hot_start(list(L4), 21)
@@ -93,12 +125,12 @@ def test_action_api_with_rectangles(pkg):
     drv = pkg.md_driver(U, a, steps=4)
     p = drv.params()
     assert p.beta == pytest.approx(2 * CP) and p.c_rect == pytest.approx(CR)
-    with pytest.raises(ValueError):
-        pkg.md_driver(U, a, steps=4, precision="mixed")
     net = pkg.CovNeuralnet()
     pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
-    with pytest.raises(ValueError):
-        pkg.md_driver(U, a, steps=4, smearing=net)
+    for prec in ("mixed", "dfloat"):
+        for sm in (None, net):
+            p = pkg.md_driver(U, a, steps=4, precision=prec, smearing=sm).params()
+            assert p.c_rect == pytest.approx(CR) and p.nstout == (0 if sm is None else 1)
 
 
 def test_sexton_weingarten_with_a_rectangle_member(md, oracle):
@@ -190,25 +222,159 @@ def test_iwasaki_trajectory_matches_the_oracle(pkg, oracle, integrator):
     assert du < 1e-12 and dp < 1e-12
 
 
-@pytest.mark.gpu
-def test_rectangle_term_is_refused_outside_the_plain_form(pkg):
+def _dfloat_force(pkg, U, a, eps):
+    """P = eps F(U) through gf_md_mom_update in the double-float form."""
     from gaugefields_gb300 import _lib
     import ctypes
-    U = pkg.gauge_configuration(L4, start="hot", seed=1)
     P = pkg.gauge_momenta(U)
+    p = pkg.md_driver(U, a, steps=2, precision="dfloat").params()
+    _lib.call("gf_md_mom_update", U.ctx.h, P.field.h, U.field.h, ctypes.c_double(eps), ctypes.byref(p), ctx=U.ctx.h)
+    return P.to_host()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L", [(8, 8, 8, 8), L6])
+def test_dfloat_rectangle_force_matches_the_oracle(pkg, oracle, L):
+    """The double-float plaquette + rectangle force (k_force_rect_df): 84
+    fixed-grid products per link, each carrying ~2^-44 (6e-14) of its
+    operands' norms through chains of four products and 24 staples weighted
+    by c_plaq = 4.2, c_rect = -0.38; the force (|F| ~ 10 at beta = 2.3 on a
+    Haar start) agrees with the fp64 oracle to 1e-12 of max |F| (measured
+    3.6e-13). A momentum step with eps = -0.5 adds -0.5 F to the zero momenta
+    (keep = 1 path)."""
+    U = pkg.gauge_configuration(L, start="hot", seed=33)
+    Uh = U.to_host()
     a = pkg.GaugeAction(U)
     pkg.push_(a, CP, "plaquette")
     pkg.push_(a, CR, "rectangular")
-    p = pkg.md_driver(U, a, steps=2).params()
-    p.precision = _lib.GF_MIXED
-    with pytest.raises(Exception):
-        _lib.call("gf_md_mom_update", U.ctx.h, P.field.h, U.field.h, ctypes.c_double(0.1), ctypes.byref(p),
-                  ctx=U.ctx.h)
-    p.precision = _lib.GF_FP64
-    p.nstout, p.rho[0] = 1, 0.1
-    with pytest.raises(Exception):
-        _lib.call("gf_md_mom_update", U.ctx.h, P.field.h, U.field.h, ctypes.c_double(0.1), ctypes.byref(p),
-                  ctx=U.ctx.h)
+    ref = oracle.force_loops(list(L), Uh, CP, CR)
+    F = _dfloat_force(pkg, U, a, 1.0)
+    dF = np.abs(F - ref).max()
+    Fh = _dfloat_force(pkg, U, a, -0.5)
+    dFh = np.abs(Fh + 0.5 * ref).max()
+    print("dfloat rectangle %s: |F| %.3f  |dF| %.2e  half step %.2e" % (L, np.abs(ref).max(), dF, dFh))
+    fmax = np.abs(ref).max()
+    assert dF < 1e-12 * fmax and dFh < 0.5e-12 * fmax
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("integrator", ["QPQ", "PQP"])
+def test_dfloat_iwasaki_trajectory_tracks_the_plain_form(pkg, integrator):
+    """8^4 Haar start, Iwasaki beta = 2.3, tau = 0.5, 10 steps: the
+    double-float form (rectangle force and link updates in double-float)
+    against the plain fp64 form from the same start: Delta H to 1e-9 (the
+    form's bound is 1e-4), links and momenta to 1e-11."""
+    U = pkg.gauge_configuration((8, 8, 8, 8), start="hot", seed=43)
+    P = pkg.gaussian_momenta(U, seed=44)
+    Uh, Ph = U.to_host(), P.to_host()
+    res = {}
+    for prec in ("fp64", "dfloat"):
+        U.from_host(Uh)
+        P.from_host(Ph)
+        a = pkg.GaugeAction(U)
+        pkg.push_(a, CP, "plaquette")
+        pkg.push_(a, CR, "rectangular")
+        integ = pkg.QPQ() if integrator == "QPQ" else pkg.PQP()
+        drv = pkg.md_driver(U, a, steps=10, trajectory_length=0.5, integrator=integ, precision=prec)
+        r = pkg.md_trajectory_(U, P, drv)
+        res[prec] = (r.delta_hamiltonian, U.to_host(), P.to_host())
+    ddh = abs(res["dfloat"][0] - res["fp64"][0])
+    du = np.abs(res["dfloat"][1] - res["fp64"][1]).max()
+    dp = np.abs(res["dfloat"][2] - res["fp64"][2]).max()
+    print("dfloat iwasaki %s: dH %.6e fp64 %.6e  |ddH| %.2e |dU| %.2e |dP| %.2e"
+          % (integrator, res["dfloat"][0], res["fp64"][0], ddh, du, dp))
+    assert ddh < 1e-9 and du < 1e-11 and dp < 1e-11
+
+
+def _iwasaki(pkg, U):
+    a = pkg.GaugeAction(U)
+    pkg.push_(a, CP, "plaquette")
+    pkg.push_(a, CR, "rectangular")
+    return a
+
+
+@pytest.mark.gpu
+def test_mixed_rectangle_force_is_close(pkg, oracle):
+    """The mixed form's plaquette + rectangle force: fp32 staples on the
+    12-real fp32 links, against the fp64 oracle to 1e-5 of max |F|."""
+    U = pkg.gauge_configuration(L6, start="hot", seed=35)
+    Uh = U.to_host()
+    P = pkg.gauge_momenta(U)
+    pkg.update_momenta_(P, U, 1.0, pkg.md_driver(U, _iwasaki(pkg, U), steps=1, precision="mixed"))
+    ref = oracle.force_loops(list(L6), Uh, CP, CR)
+    rel = np.abs(P.to_host() - ref).max() / np.abs(ref).max()
+    print("mixed rectangle force: rel %.2e" % rel)
+    assert rel < 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("dfloat", 1e-11), ("mixed", 1e-5)])
+def test_smeared_rectangle_force_matches_the_oracle(pkg, oracle, prec, tol):
+    """Two stout levels (rho = 0.1) under the Iwasaki action at 8^4: the top
+    level's loop-set dS/dUbar (k_dsdu_rect, or k_force_rect_df writing it
+    double-float-native), back-propagated by the stout adjoint of the form,
+    against the oracle; tolerance relative to max |F| (fp64 1e-12,
+    double-float 1e-11, mixed 1e-5)."""
+    L = (8, 8, 8, 8)
+    U = pkg.gauge_configuration(L, start="hot", seed=36)
+    Uh = U.to_host()
+    net = pkg.CovNeuralnet(U)
+    pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
+    pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
+    P = pkg.gauge_momenta(U)
+    pkg.update_momenta_(P, U, 1.0, pkg.md_driver(U, _iwasaki(pkg, U), steps=1, smearing=net, precision=prec))
+    ref = oracle.stout_force_loops(list(L), Uh, (0.1, 0.1), CP, CR)
+    rel = np.abs(P.to_host() - ref).max() / np.abs(ref).max()
+    print("smeared rectangle force %s: |F| %.3f rel %.2e" % (prec, np.abs(ref).max(), rel))
+    assert rel < tol
+
+
+@pytest.mark.gpu
+def test_smeared_iwasaki_trajectory_matches_the_oracle(pkg, oracle):
+    """4^4 Haar start, one stout level under the Iwasaki action, tau = 0.3,
+    6 QPQ steps in the plain form: H0 to 1e-13 relative, Delta H to 1e-10,
+    links to 1e-12 against the oracle with a full-double-precision
+    exponential."""
+    U = pkg.gauge_configuration(L4, start="hot", seed=45)
+    P = pkg.gaussian_momenta(U, seed=46)
+    Uh, Ph = U.to_host(), P.to_host()
+    net = pkg.CovNeuralnet(U)
+    pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
+    drv = pkg.md_driver(U, _iwasaki(pkg, U), steps=6, trajectory_length=0.3, smearing=net, reunitarize=False)
+    res = pkg.md_trajectory_(U, P, drv)
+    oracle.set_exp_method("taylor")
+    try:
+        h = oracle.md_trajectory(list(L4), Uh, Ph, 2 * CP, 0.3, 6, "QPQ", rho=(0.1,), c_rect=CR)
+    finally:
+        oracle.set_exp_method("eigen")
+    du = np.abs(U.to_host() - Uh).max()
+    print("smeared iwasaki: dH %.6e oracle %.6e |dU| %.2e" % (res.delta_hamiltonian, h[2], du))
+    assert abs(res.initial_hamiltonian - h[0]) <= 1e-13 * abs(h[0])
+    assert abs(res.delta_hamiltonian - h[2]) <= 1e-10
+    assert du < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec,tol", [("dfloat", 1e-8), ("mixed", 2e-2)])
+def test_smeared_iwasaki_forms_track_the_plain_form(pkg, prec, tol):
+    """8^4 Haar start, two stout levels under the Iwasaki action, tau = 0.5,
+    10 steps: Delta H of the double-float form within 1e-8 of the plain
+    form's; the mixed form's (fp32 force and adjoint) within 2e-2 at this
+    volume."""
+    U = pkg.gauge_configuration((8, 8, 8, 8), start="hot", seed=47)
+    P = pkg.gaussian_momenta(U, seed=48)
+    Uh, Ph = U.to_host(), P.to_host()
+    dh = {}
+    for form in ("fp64", prec):
+        U.from_host(Uh)
+        P.from_host(Ph)
+        net = pkg.CovNeuralnet(U)
+        pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
+        pkg.push_(net, pkg.STOUT_Layer("plaquette", 0.1))
+        drv = pkg.md_driver(U, _iwasaki(pkg, U), steps=10, trajectory_length=0.5, smearing=net, precision=form)
+        dh[form] = pkg.md_trajectory_(U, P, drv).delta_hamiltonian
+    print("smeared iwasaki %s: dH %.6e fp64 %.6e diff %.2e" % (prec, dh[prec], dh["fp64"], abs(dh[prec] - dh["fp64"])))
+    assert abs(dh[prec] - dh["fp64"]) < tol
 
 
 # ---------------------------------------------------------------------------
