@@ -239,6 +239,14 @@ __global__ void __launch_bounds__(128, GF_MINB_ADJ(R))
 #ifndef GF_DF_GRID
 #define GF_DF_GRID 1
 #endif
+// Table products leave their slot entries normalised (1) or as raw grid pairs
+// (0). At 32^4 the raw pairs measured 1.92 trajectories/s against 1.84
+// (1.95 together with GF_DF_DAG_LOAD = 1), with about ten times the error:
+// the stout force 1e-10 of the fp64 oracle's instead of 1e-11. The default
+// keeps the accuracy.
+#ifndef GF_DF_NORM
+#define GF_DF_NORM 1
+#endif
 
 struct DfOp {
   // src: 0, 1, 2 fields F0, F1, F2, 3 + k slot k; dir: 0 the kernel's link
@@ -261,15 +269,52 @@ struct DfFields {
   const float4* f1;
   const float4* f2;
 };
+// Daggered operands: GF_DF_DAG_LOAD = 1 takes the transposition in the load
+// addresses (element (i, j) of M^dag is read from (j, i)) and negates the
+// imaginary parts after the loads; 0 loads M and forms dag(M) in registers.
+// Same results; at 32^4 the address form measured 0.4% slower per trajectory
+// alone (gather slower, local adjoint faster) and 1.5% faster with raw pairs.
+#ifndef GF_DF_DAG_LOAD
+#define GF_DF_DAG_LOAD 0
+#endif
+__device__ __forceinline__ int op_elem(int e, int dagger) { return dagger ? (e % 3) * 3 + e / 3 : e; }
 template <typename E0>
 __device__ __forceinline__ mat3<dfl> df_operand(int src, int dir, int site, int dagger, const float* sm, int tid,
                                                 const DfFields<E0>& F, int V, int d0, int d1, const DfSites& st) {
   mat3<dfl> m;
   const int mu = dir ? d1 : d0, x = pick_site(st, site);
+#if GF_DF_DAG_LOAD
+  if (src == 0 && !std::is_same<E0, float4>::value) {
+    m = DfIO<E0>::load(F.f0, mu, x, V);
+    if (dagger) m = dag(m);
+    return m;
+  }
+  if (src >= 3) {
+    const float4* q = reinterpret_cast<const float4*>(sm) + (src - 3) * 9 * 128 + tid;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) {
+      const float4 v = q[op_elem(e, dagger) * 128];
+      m.e[e / 3][e % 3] = mk(dfl(v.x, v.y), dfl(v.z, v.w));
+    }
+  } else {
+    const float4* f = src == 0 ? reinterpret_cast<const float4*>(F.f0) : (src == 1 ? F.f1 : F.f2);
+    const float4* b = f + (size_t)mu * 9 * V + x;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) {
+      const float4 v = __ldg(b + (size_t)op_elem(e, dagger) * V);
+      m.e[e / 3][e % 3] = mk(dfl(v.x, v.y), dfl(v.z, v.w));
+    }
+  }
+  if (dagger) {
+#pragma unroll
+    for (int e = 0; e < 9; ++e) m.e[e / 3][e % 3].im = dfl(-m.e[e / 3][e % 3].im.hi, -m.e[e / 3][e % 3].im.lo);
+  }
+#else
   if (src >= 3) m = slot_load(sm, src - 3, tid);
   else if (src == 0) m = DfIO<E0>::load(F.f0, mu, x, V);
   else m = LinkDfn::load(src == 1 ? F.f1 : F.f2, mu, x, V);
   if (dagger) m = dag(m);
+#endif
   return m;
 }
 template <typename E0>
@@ -282,7 +327,7 @@ __device__ __forceinline__ void df_exec(const DfOp op, float* sm, int tid, const
   // 3% slower per trajectory (larger body)
   const mat3<dfl> C = op.accumulate ? slot_load(sm, op.out, tid) : zero3<dfl>();
 #if GF_DF_GRID
-  slot_store(sm, op.out, tid, dfg_matmul<false, false, true>(A, B, &C));
+  slot_store(sm, op.out, tid, dfg_matmul<false, false, true, 3, GF_DF_NORM>(A, B, &C));
 #else
   slot_store(sm, op.out, tid, df_matmul<false, false, true>(A, B, &C));
 #endif

@@ -769,7 +769,13 @@ GF_HD void grid_term(float& A, float& L, float xh, float xl, float yh, float yl)
   A = An;
 }
 
-template <bool DA, bool DB, bool ACC, int ROWS = 3>
+//
+// NORM = false leaves each entry as the raw pair (A - K, L) instead of the
+// normalised double-float fast_two_sum(A - K, L): the same value, with a low
+// word of up to ~2^-19 of the bound instead of half an ulp of the high word.
+// The next product's grid sees only high words, so it stays exact; its cross
+// terms carry the larger low word at fp32 precision (~2^-43 instead of ~2^-44).
+template <bool DA, bool DB, bool ACC, int ROWS = 3, bool NORM = true>
 GF_HD mat3<dfl> dfg_matmul(const mat3<dfl>& a, const mat3<dfl>& b, const mat3<dfl>* c) {
   float ra = 0.f, cb = 0.f;
 #pragma unroll
@@ -817,7 +823,8 @@ GF_HD mat3<dfl> dfg_matmul(const mat3<dfl>& a, const mat3<dfl>& b, const mat3<df
         grid_term(Ai, Li, x.re.hi, x.re.lo, y.im.hi, y.im.lo);
         grid_term(Ai, Li, x.im.hi, x.im.lo, y.re.hi, y.re.lo);
       }
-      r.e[i][j] = mk(df_fast_two_sum(Ar - K, Lr), df_fast_two_sum(Ai - K, Li));
+      if (NORM) r.e[i][j] = mk(df_fast_two_sum(Ar - K, Lr), df_fast_two_sum(Ai - K, Li));
+      else r.e[i][j] = mk(dfl(Ar - K, Lr), dfl(Ai - K, Li));
     }
   return r;
 }
