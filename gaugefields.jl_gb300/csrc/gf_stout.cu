@@ -239,14 +239,6 @@ __global__ void __launch_bounds__(128, GF_MINB_ADJ(R))
 #ifndef GF_DF_GRID
 #define GF_DF_GRID 1
 #endif
-// Table products leave their slot entries normalised (1) or as raw grid pairs
-// (0). At 32^4 the raw pairs measured 1.92 trajectories/s against 1.84
-// (1.95 together with GF_DF_DAG_LOAD = 1), with about ten times the error:
-// the stout force 1e-10 of the fp64 oracle's instead of 1e-11. The default
-// keeps the accuracy.
-#ifndef GF_DF_NORM
-#define GF_DF_NORM 1
-#endif
 
 struct DfOp {
   // src: 0, 1, 2 fields F0, F1, F2, 3 + k slot k; dir: 0 the kernel's link
@@ -273,7 +265,8 @@ struct DfFields {
 // addresses (element (i, j) of M^dag is read from (j, i)) and negates the
 // imaginary parts after the loads; 0 loads M and forms dag(M) in registers.
 // Same results; at 32^4 the address form measured 0.4% slower per trajectory
-// alone (gather slower, local adjoint faster) and 1.5% faster with raw pairs.
+// alone (gather slower, local adjoint faster) and 2% faster with raw pairs
+// (GF_DF_NORM = 0).
 #ifndef GF_DF_DAG_LOAD
 #define GF_DF_DAG_LOAD 0
 #endif
@@ -382,7 +375,7 @@ __global__ void __launch_bounds__(128, GF_DF_GATHER_MINB)
   }
   if (!live) return;
   mat3<dfl> d = LinkDfn::load(Dp, nu, s, V);
-  axpy_to(d, rho, slot_load(sm, 1, tid));
+  axpy_to(d, rho, slot_load_n(sm, 1, tid));
   if (FORCE) {
     const mat3<dfl> M = mul_nn(LinkDfn::load(U, nu, s, V), d);
     dfl c[8];
@@ -439,13 +432,13 @@ __global__ void __launch_bounds__(128, GF_DF_FWD_MINB)
     }
     if (q == 13) {
       // Q = TA(rho S^dag U^dag) = -rho TA(U S): exp(Q) = exp(i Qh), Qh = i rho TA(U S)
-      const mat3<dfl> qh = times_i(rho, ta_proj(slot_load(sm, 0, tid)));
+      const mat3<dfl> qh = times_i(rho, ta_proj(slot_load_n(sm, 0, tid)));
       slot_store(sm, 0, tid, expiq(qh));
-      if (Cout && live) LinkDfn::store(Cout, mu, s, V, scale(rho, dag(slot_load(sm, 1, tid))));
+      if (Cout && live) LinkDfn::store(Cout, mu, s, V, scale(rho, dag(slot_load_n(sm, 1, tid))));
     }
     df_exec(c_stout_ops[q < 12 ? (q & 3) : q - 8], sm, tid, DfFields<EIN>{U, nullptr, nullptr}, V, mu, nu, ss);
   }
-  if (live) LinkDfn::store(Uout, mu, s, V, slot_load(sm, 1, tid));
+  if (live) LinkDfn::store(Uout, mu, s, V, slot_load_n(sm, 1, tid));
 }
 
 // The coefficient algebra of the double-float local adjoint, as fixed-grid
@@ -565,11 +558,11 @@ __global__ void __launch_bounds__(128, TOP ? GF_MINB_ADJ(dfl) : GF_DF_LOCAL_MINB
     if (op.a_src == 15) op.a_src = TOP ? 7 : 1;
     if (op.b_src == 15) op.b_src = TOP ? 7 : 1;
     df_exec(op, sm, tid, F, V, mu, nu, ss);
-    if (q == 11) slot_store(sm, 5, tid, scale(rho, dag(slot_load(sm, 5, tid))));  // C = rho S^dag
-    if (q == 23) slot_store(sm, 4, tid, scale(halfbeta, slot_load(sm, 4, tid)));  // Dbar = beta/2 S
+    if (q == 11) slot_store(sm, 5, tid, scale(rho, dag(slot_load_n(sm, 5, tid))));  // C = rho S^dag
+    if (q == 23) slot_store(sm, 4, tid, scale(halfbeta, slot_load_n(sm, 4, tid)));  // Dbar = beta/2 S
     if (q == 24) {
       // Qh = -i TA(C U^dag)
-      const mat3<dfl> qh = times_i(dfl(-1), ta_proj(slot_load(sm, 0, tid)));
+      const mat3<dfl> qh = times_i(dfl(-1), ta_proj(slot_load_n(sm, 0, tid)));
       dfl c0, c1;
       herm_invariants(qh, c0, c1);
       ch_coefficients<dfl, true>(c0, c1, cc);
@@ -577,16 +570,16 @@ __global__ void __launch_bounds__(128, TOP ? GF_MINB_ADJ(dfl) : GF_DF_LOCAL_MINB
       slot_store(sm, 2, tid, herm_square(qh));
     }
     if (q == 27) {
-      const mat3<dfl> lam = slot_load(sm, 3, tid), qh = slot_load(sm, 1, tid), qh2 = slot_load(sm, 2, tid);
-      mat3<dfl> gam = slot_load(sm, 0, tid);
+      const mat3<dfl> lam = slot_load_n(sm, 3, tid), qh = slot_load(sm, 1, tid), qh2 = slot_load(sm, 2, tid);
+      mat3<dfl> gam = slot_load_n(sm, 0, tid);
       mat3<dfl> E;
       df_gamma_and_exp(cc, lam, qh, qh2, gam, E);
       slot_store(sm, 0, tid, ta_proj(times_i(dfl(-1), gam)));  // Y
       slot_store(sm, 2, tid, E);                                // e^Q
     }
-    if (q == 28 && live) LinkDfn::store(Zout, mu, s, V, slot_load(sm, 3, tid));
+    if (q == 28 && live) LinkDfn::store(Zout, mu, s, V, slot_load_n(sm, 3, tid));
   }
-  if (live) LinkDfn::store(Dpout, mu, s, V, slot_load(sm, 3, tid));
+  if (live) LinkDfn::store(Dpout, mu, s, V, slot_load_n(sm, 3, tid));
 }
 
 // --------------------------------------------------------------------------

@@ -642,7 +642,7 @@ __device__ __forceinline__ cplx<R> ch_combine(const ch_coef<R>& cc, const mat3<R
 // rebuilt or not stored. OPS = true combines f0 + f1 Q + f2 Q^2 with the
 // type's operators (for double-float: the accurate double-word sums, ~2^-48,
 // which chains of link updates keep to 1e-12 of fp64), false with the
-// fixed-grid sum (~2^-44 of the bound) where one is given.
+// fixed-grid sum (rms ~2^-43 of the bound) where one is given.
 template <typename R, int ROWS = 3, bool OPS = false>
 __device__ __forceinline__ mat3<R> expiq(const mat3<R>& q, mat3<R>* q2out = nullptr) {
   R c0, c1;
@@ -734,8 +734,9 @@ GF_HD mat3<dfl> df_matmul(const mat3<dfl>& a, const mat3<dfl>& b, const mat3<dfl
 // a_h b_h + (A - A_new) (about 24 bits, exact to 2^-48 relative). Residuals
 // and the cross terms a_h b_l + a_l b_h go to a plain fp32 correction. Six
 // fp32 operations per real term instead of the twelve of the TwoSum-based
-// accumulation above; the error is ~2^-44 of |op(A)| |op(B)| (+ |C|) per
-// entry, against ~2^-48 there. The bound: partial sums of entry (i,j) are at
+// accumulation above; the error per entry is rms ~2^-43 and at most ~2^-38
+// of |op(A)| |op(B)| (+ |C|) (the correction word sums up to twelve
+// residuals of half a grid step in fp32), against rms ~2^-48 there. The bound: partial sums of entry (i,j) are at
 // most |row i of op(A)| |column j of op(B)| (Cauchy-Schwarz), so
 // M^2 = max_i |a_i|^2 max_j |b_j|^2 (+ the accumulator's entries), and k is
 // taken from M^2's exponent with a factor 2 of headroom.
@@ -774,7 +775,7 @@ GF_HD void grid_term(float& A, float& L, float xh, float xl, float yh, float yl)
 // normalised double-float fast_two_sum(A - K, L): the same value, with a low
 // word of up to ~2^-19 of the bound instead of half an ulp of the high word.
 // The next product's grid sees only high words, so it stays exact; its cross
-// terms carry the larger low word at fp32 precision (~2^-43 instead of ~2^-44).
+// terms carry the larger low word at fp32 precision (rms 1.5x the error).
 template <bool DA, bool DB, bool ACC, int ROWS = 3, bool NORM = true>
 GF_HD mat3<dfl> dfg_matmul(const mat3<dfl>& a, const mat3<dfl>& b, const mat3<dfl>* c) {
   float ra = 0.f, cb = 0.f;

@@ -49,9 +49,9 @@ def test_dfloat_stout_force_matches_oracle(pkg, oracle, L):
 
 def test_dfloat_stout_force_recompute_matches_store(pkg):
     """Recomputing C in the adjoint gives the stored-C force to 1e-11 per link:
-    the two paths form C with different product kernels (the forward's table
-    loop and the local adjoint's inlined products), each accurate to ~2^-44
-    relative, so they are not bitwise equal as in the fp64 form."""
+    the two paths form C in different kernels (the forward, and the local
+    adjoint's recompute) with fixed-grid products (rms ~2^-43 of the operand
+    norms), and are not bitwise equal as in the fp64 form."""
     out = []
     for recompute in (False, True):
         U = pkg.gauge_configuration(L4, start="hot", seed=13)
@@ -161,7 +161,7 @@ def test_hamiltonian_with_alternating_level_buffers(pkg, nlev):
     """The mixed form's Hamiltonian smears with a forward-only double-float
     stack whose levels beyond the second reuse two buffers in turn; with 3 and
     4 levels it equals the fp64 Hamiltonian to 5e-13 relative (double-float
-    smearing with fixed-grid products, ~2^-44 relative per product, over 3-4
+    smearing with fixed-grid products, rms ~2^-43 relative per product, over 3-4
     levels; a reused buffer holding a wrong level would be off by ~1e-3)."""
     U = pkg.gauge_configuration(L4, start="hot", seed=19)
     P = pkg.gaussian_momenta(U, seed=20)

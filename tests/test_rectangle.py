@@ -236,7 +236,7 @@ def _dfloat_force(pkg, U, a, eps):
 @pytest.mark.parametrize("L", [(8, 8, 8, 8), L6])
 def test_dfloat_rectangle_force_matches_the_oracle(pkg, oracle, L):
     """The double-float plaquette + rectangle force (k_force_rect_df): 84
-    fixed-grid products per link, each carrying ~2^-44 (6e-14) of its
+    fixed-grid products per link, each carrying rms ~2^-43 (1.2e-13) of its
     operands' norms through chains of four products and 24 staples weighted
     by c_plaq = 4.2, c_rect = -0.38; the force (|F| ~ 10 at beta = 2.3 on a
     Haar start) agrees with the fp64 oracle to 1e-12 of max |F| (measured
