@@ -20,6 +20,9 @@ thermalised SU(3) configuration written by the reference.
 * dS/drho of each stout level on the device (gf_stout_param_derivatives)
   against the oracle's parameter_derivatives and against central differences
   of the device potential.
+* The smallest lattices the layout takes (extents of 2, fewer sites than a
+  block): plaquette, rectangle sum, Wilson, stout and rectangle forces and a
+  stout trajectory against the oracle.
 """
 import os
 
@@ -255,3 +258,42 @@ def test_stout_dsdrho_matches_finite_differences_of_the_device_potential(pkg, or
             vals.append(pkg.md_hamiltonian(U, zero, pkg.md_driver(U, action, steps=1, smearing=n)))
         fd = -3.0 * (vals[0] - vals[1]) / (2 * h)
         assert abs(got[l] - fd) <= 1e-6 * abs(fd), (l, got[l], fd)
+
+
+@pytest.mark.parametrize("L", [(2, 4, 2, 6), (2, 2, 2, 2)])
+def test_minimal_extents(pkg, oracle, exact_exp_oracle, L):
+    """Lattices with extent 2 (x + mu and x - mu are the same site; x + 2 mu
+    is x itself) and a partial block (96 or 16 sites): plaquette, rectangle
+    sum, Wilson force, the 2-level stout force in the fp64 and double-float
+    forms, the plaquette + rectangle force and one fp64 stout trajectory
+    against the oracle."""
+    U = pkg.gauge_configuration(L, start="hot", seed=61)
+    Uh = U.to_host()
+    ref = oracle.plaquette(list(L), Uh)
+    assert abs(pkg.calculate_Plaquette(U) - ref) <= 1e-13 * abs(ref)
+    rref = oracle.rectangle_sum(list(L), Uh)
+    assert abs(pkg.rectangle_sum(U) - rref) <= 1e-13 * abs(rref)
+    action = pkg.GaugeAction(U)
+    pkg.push_(action, 2.85, "plaquette")
+    F = pkg.gauge_momenta(U)
+    pkg.md_force_(F, action, U)
+    assert frob_mom(F.to_host(), oracle.force(list(L), Uh, 5.7)) < 1e-12
+    sref = oracle.stout_force(list(L), Uh, [0.1, 0.1], 6.0)
+    for prec in ("fp64", "dfloat"):
+        P = pkg.gauge_momenta(U)
+        pkg.update_momenta_(P, U, 1.0, _stout_driver(pkg, U, prec))
+        assert frob_mom(P.to_host(), sref) < 1e-11 * max(1.0, np.abs(sref).max()), prec
+    iwa = pkg.GaugeAction(U)
+    pkg.push_(iwa, 4.2, "plaquette")
+    pkg.push_(iwa, -0.38, "rectangular")
+    for prec in ("fp64", "dfloat"):
+        P = pkg.gauge_momenta(U)
+        pkg.update_momenta_(P, U, 1.0, pkg.md_driver(U, iwa, steps=1, precision=prec))
+        assert np.abs(P.to_host() - oracle.force_loops(list(L), Uh, 4.2, -0.38)).max() < 1e-11, prec
+    P = pkg.gaussian_momenta(U, seed=62)
+    Ph = P.to_host()
+    res = pkg.md_trajectory_(U, P, _stout_driver(pkg, U, "fp64", steps=4, trajectory_length=0.4,
+                                                 reunitarize=False))
+    h = exact_exp_oracle.md_trajectory(list(L), Uh, Ph, 6.0, 0.4, 4, rho=[0.1, 0.1])
+    assert abs(res.delta_hamiltonian - h[2]) <= 1e-10
+    assert frob_links(U.to_host(), Uh) < 1e-12
