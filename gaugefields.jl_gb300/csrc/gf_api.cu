@@ -556,12 +556,12 @@ static gf_stout* ctx_stout(gf_ctx* ctx, const gf_md_params* p, int precision) {
   return *slot;
 }
 
-// The potential on the (smeared) fp64 links. The plain form evaluates it in
-// fp64. The mixed and double-float forms smear in double-float arithmetic
-// (~1e-14 per operation, compensated products) on the fp32 pipes with fp64
-// storage, which on GB300 is 2.1x faster than the fp64 stout forward; the
-// plaquette sum over the smeared links stays fp64 (GF_DF_HAMILTONIAN=0 keeps
-// the mixed form's potential fp64).
+// The potential on the (smeared) fp64 links, plaquette and rectangle loops.
+// The plain form evaluates it in fp64. The mixed and double-float forms smear
+// in double-float arithmetic (compensated products, ~1e-13 of the operands'
+// norms) on the fp32 pipes, which on GB300 is 2.1x faster than the fp64 stout
+// forward; the loop sums over the smeared links stay fp64
+// (GF_DF_HAMILTONIAN=0 keeps the mixed form's potential fp64).
 #ifndef GF_DF_HAMILTONIAN
 #define GF_DF_HAMILTONIAN 1
 #endif
