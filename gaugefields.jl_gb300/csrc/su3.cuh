@@ -776,6 +776,36 @@ GF_HD void grid_term(float& A, float& L, float xh, float xl, float yh, float yl)
 // word of up to ~2^-19 of the bound instead of half an ulp of the high word.
 // The next product's grid sees only high words, so it stays exact; its cross
 // terms carry the larger low word at fp32 precision (rms 1.5x the error).
+//
+// GF_DF_PACKED = 1 runs the real and imaginary accumulators of an entry as one
+// pair through the paired fp32 instructions of sm_100-class GPUs (__ffma2_rn,
+// __fadd2_rn; per component the same correctly rounded operations as fmaf and
+// +), the terms of each accumulator in the scalar order, so the results are
+// bitwise those of the scalar form with half the arithmetic instructions. The
+// operand pairs (x.re, x.re), (-x.im, x.im), (y.re, y.im), (y.im, y.re) are
+// rebuilt with moves for every term, and at 32^4 the paired form measured
+// 1.55 trajectories/s against 1.84 (gather 6.3 against 4.9 ms, small spills
+// at the gather's 128 registers), so the scalar form is the default.
+#ifndef GF_DF_PACKED
+#define GF_DF_PACKED 0
+#endif
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000 && GF_DF_PACKED
+#define GF_DF_PAIRED 1
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+// grid_term on the pair (re, im): the same six operations per component
+__device__ __forceinline__ void grid_term2(float2& A, float2& L, float2 xh, float2 xl, float2 yh, float2 yl) {
+  const float2 An = __ffma2_rn(xh, yh, A);
+  const float2 t = __fadd2_rn(A, neg2(An));
+  L = __fadd2_rn(L, __ffma2_rn(xh, yh, t));
+  L = __ffma2_rn(xh, yl, L);
+  L = __ffma2_rn(xl, yh, L);
+  A = An;
+}
+#else
+#define GF_DF_PAIRED 0
+#endif
+
 template <bool DA, bool DB, bool ACC, int ROWS = 3, bool NORM = true>
 GF_HD mat3<dfl> dfg_matmul(const mat3<dfl>& a, const mat3<dfl>& b, const mat3<dfl>* c) {
   float ra = 0.f, cb = 0.f;
@@ -803,6 +833,39 @@ GF_HD mat3<dfl> dfg_matmul(const mat3<dfl>& a, const mat3<dfl>& b, const mat3<df
   }
   const float K = df_grid_const(m2);
   mat3<dfl> r = zero3<dfl>();
+#if GF_DF_PAIRED
+  const float2 K2 = f2(K, K);
+#pragma unroll
+  for (int i = 0; i < ROWS; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      float2 A2 = K2, L2 = f2(0.f, 0.f);
+      if (ACC) {
+        const cplx<dfl> v = c->e[i][j];
+        const float2 vh = f2(v.re.hi, v.im.hi);
+        A2 = __fadd2_rn(K2, vh);
+        L2 = __fadd2_rn(__fadd2_rn(vh, neg2(__fadd2_rn(A2, neg2(K2)))), f2(v.re.lo, v.im.lo));
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const cplx<dfl> x = DA ? conj(a.e[k][i]) : a.e[i][k];
+        const cplx<dfl> y = DB ? conj(b.e[j][k]) : b.e[k][j];
+        // (re, im) += (x.re y.re, x.re y.im), then (-x.im y.im, x.im y.re)
+        grid_term2(A2, L2, f2(x.re.hi, x.re.hi), f2(x.re.lo, x.re.lo), f2(y.re.hi, y.im.hi), f2(y.re.lo, y.im.lo));
+        grid_term2(A2, L2, f2(-x.im.hi, x.im.hi), f2(-x.im.lo, x.im.lo), f2(y.im.hi, y.re.hi),
+                   f2(y.im.lo, y.re.lo));
+      }
+      const float2 sv = __fadd2_rn(A2, neg2(K2));
+      if (NORM) {
+        const float2 h = __fadd2_rn(sv, L2);
+        const float2 e = __fadd2_rn(L2, neg2(__fadd2_rn(h, neg2(sv))));
+        r.e[i][j] = mk(dfl(h.x, e.x), dfl(h.y, e.y));
+      } else {
+        r.e[i][j] = mk(dfl(sv.x, L2.x), dfl(sv.y, L2.y));
+      }
+    }
+  return r;
+#else
 #pragma unroll
   for (int i = 0; i < ROWS; ++i)
 #pragma unroll
@@ -828,6 +891,7 @@ GF_HD mat3<dfl> dfg_matmul(const mat3<dfl>& a, const mat3<dfl>& b, const mat3<df
       else r.e[i][j] = mk(dfl(Ar - K, Lr), dfl(Ai - K, Li));
     }
   return r;
+#endif
 }
 
 // Fixed-grid accumulators for single sums of products (traces, Q^2 and the
