@@ -187,6 +187,16 @@ def read_peaks():
     return 6800.0, "of fallback (6.8 TB/s)"
 
 
+def read_utilisation(kclass):
+    """The binding unit's utilisation of a kernel class (issue slots for the
+    double-float kernels, the fp64 pipe for the fp64 ones) from the committed
+    ncu summaries, as [metric, fraction]."""
+    p = os.path.join(ROOT, "profiles", "utilisation.json")
+    if not os.path.exists(p):
+        return None
+    return json.load(open(p)).get(kclass)
+
+
 def read_traffic(kclass, L):
     """DRAM bytes per launch of a kernel class from the committed ncu summary."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
@@ -430,6 +440,10 @@ def roofline_of(kern, V, L, peaks, hbm_peak, hbm_note):
     compute = {"kernel": dom, "precision": prec, "achieved_tflops": tf, "peak_tflops": pk, "peak_note": note,
                "flops_per_launch": fl, "frac": tf / pk,
                "binding": {"fp64": "fp64 issue", "fp32": "fp32 issue / L1", "df": "fp32 issue"}[prec]}
+    util = read_utilisation(dom)
+    if util:
+        compute["ncu_utilisation"] = {"metric": util[0], "value": util[1],
+                                      "note": "one launch at 24^4 in the committed ncu capture"}
     if prec == "df":
         compute["fp32_ops_tflops"] = 3.0 * tf
         compute["fp32_frac"] = 3.0 * tf / peaks["fp32_tflops"]
