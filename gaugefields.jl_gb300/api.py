@@ -28,7 +28,7 @@ __all__ = [
     "hmc_update_", "STOUT_Layer", "CovNeuralnet", "stout_smearing", "smear", "calc_smearedU", "back_prop",
     "get_parameter_derivatives",
     "Gradientflow", "gradient_flow", "flow_", "add_force_", "energy_density_plaquette", "substitute_U_",
-    "similar", "clear_U_", "normalize_U_", "save_configuration", "load_configuration_", "Oneinstanton_SUN_embedded",
+    "similar", "clear_U_", "normalize_U_", "copy_configuration_", "copy_configuration", "save_configuration", "load_configuration_", "Oneinstanton_SUN_embedded",
     "MDActionSet", "MDForceGroup", "SextonWeingarten", "rectangle_sum", "Gradientflow_general",
 ]
 
@@ -299,6 +299,27 @@ def similar(U):
 def substitute_U_(A, B):
     """substitute_U!(A, B): A <- B (src/4D/mpi_jacc/gaugefields_4D_MPILattice.jl:509)."""
     call("gf_field_copy", A.ctx.h, A.field.h, B.field.h, ctx=A.ctx.h)
+
+
+def copy_configuration_(destination, source):
+    """copy_configuration!(destination, source) (src/API.jl:300-322): a
+    complete configuration into compatible storage, returned. Different
+    numbers of directions or lattice sizes raise (the reference's
+    DimensionMismatch, a ValueError here)."""
+    if len(destination) != len(source):
+        raise ValueError("destination and source have different numbers of directions")
+    if tuple(destination.L) != tuple(source.L):
+        raise ValueError("destination and source lattice sizes differ")
+    if destination.ctx is not source.ctx:
+        destination.from_host(source.to_host())
+    else:
+        substitute_U_(destination, source)
+    return destination
+
+
+def copy_configuration(source):
+    """copy_configuration(source) (src/API.jl:324-328): an independent copy."""
+    return copy_configuration_(similar(source), source)
 
 
 def clear_U_(A):

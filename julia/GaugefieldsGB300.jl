@@ -38,7 +38,8 @@ using LinearAlgebra
 using Gaugefields
 import Gaugefields: md_action_workspace, md_potential, md_force!, md_hamiltonian, update_momenta!,
                     update_gaugefields!, md_trajectory!, md_step!, gauge_configuration, gaussian_momenta!,
-                    calculate_Plaquette, substitute_U!, clear_U!, initialize_TA_Gaugefields, back_prop
+                    calculate_Plaquette, substitute_U!, clear_U!, initialize_TA_Gaugefields, back_prop,
+                    copy_configuration!, copy_configuration
 import Gaugefields.AbstractGaugefields_module: Gaugefields_4D, TA_Gaugefields_4D
 import Gaugefields.Abstractsmearing_module: CovLayer, apply_layer!, layer_pullback!, parameter_derivatives
 import Gaugefields.Gradientflow_module: Gradientflow, flow!
@@ -208,6 +209,21 @@ function substitute_U!(A::GB300Config, B::GB300Config)
                 config_field(B).h), ctx)
     return A
 end
+# copy_configuration!(destination, source) / copy_configuration(source)
+# (src/API.jl:300-328): one device copy of the shared four-direction field
+function copy_configuration!(destination::GB300Config, source::GB300Config)
+    length(destination) == length(source) ||
+        throw(DimensionMismatch("destination and source have different numbers of directions"))
+    destination[1].ctx.L == source[1].ctx.L || throw(DimensionMismatch("destination and source lattice sizes differ"))
+    if destination[1].ctx === source[1].ctx
+        substitute_U!(destination, source)
+    else
+        upload!(destination, download(source))
+    end
+    return destination
+end
+copy_configuration(source::GB300Config) = copy_configuration!(similar(source), source)
+
 function clear_U!(P::GB300Momenta)
     ctx = P[1].ctx
     check(ccall((:gf_field_zero, libgf), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx.h, momenta_field(P).h), ctx)

@@ -53,6 +53,23 @@ def test_upload_download_roundtrip_is_exact(pkg, oracle):
     assert np.array_equal(P.to_host(), B)
 
 
+def test_copy_configuration(pkg):
+    """copy_configuration / copy_configuration! (src/API.jl:300-328, the
+    reference's test/high_level_api.jl:132-155): an independent copy, the
+    destination returned, within one context and across contexts; different
+    lattice sizes raise."""
+    U = pkg.gauge_configuration(L4, start="hot", seed=71)
+    A = U.to_host()
+    V = pkg.copy_configuration(U)
+    assert V is not U and np.array_equal(V.to_host(), A)
+    U.from_host(pkg.gauge_configuration(L4, start="hot", seed=72).to_host())
+    assert np.array_equal(V.to_host(), A)
+    W = pkg.gauge_configuration(L4, start="cold")
+    assert pkg.copy_configuration_(W, V) is W and np.array_equal(W.to_host(), A)
+    with pytest.raises(ValueError):
+        pkg.copy_configuration_(pkg.gauge_configuration((4, 4, 4, 6), start="cold"), V)
+
+
 def test_cold_start_invariants(pkg):
     U = pkg.gauge_configuration(L8, start="cold")
     assert pkg.measure_plaquette(U) == 1.0
