@@ -87,6 +87,7 @@ GB300Backend() = GB300Backend(0)
 mutable struct Ctx
     h::Ptr{Cvoid}
     L::NTuple{4,Int}
+    device::Int
 end
 
 last_error(h::Ptr{Cvoid}) = unsafe_string(ccall((:gf_last_error, libgf), Cstring, (Ptr{Cvoid},), h))
@@ -103,7 +104,7 @@ end
 function Ctx(L::NTuple{4,Int}, device::Int)
     h = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:gf_ctx_create, libgf), Cint, (Ptr{Cint}, Cint, Ref{Ptr{Cvoid}}), Cint[L...], device, h))
-    c = Ctx(h[], L)
+    c = Ctx(h[], L, device)
     finalizer(x -> ccall((:gf_ctx_destroy, libgf), Cint, (Ptr{Cvoid},), x.h), c)
     return c
 end
@@ -190,6 +191,13 @@ function momenta_field(P::GB300Momenta)
     all(p -> p.field === f, P) || throw(ArgumentError("the four directions must share one GB300 momentum field"))
     return f
 end
+
+# the reference's configuration accessors (src/API.jl:262-295): the size of a
+# direction as (NC, NC, NX, NY, NZ, NT), no halo (neighbours come from index
+# arithmetic), one process
+Base.size(u::Gaugefields_4D_GB300) = (u.NC, u.NC, u.NX, u.NY, u.NZ, u.NT)
+Gaugefields.gauge_backend(u::Gaugefields_4D_GB300) = GB300Backend(u.ctx.device)
+Gaugefields.gauge_halo_width(::Gaugefields_4D_GB300) = 0
 
 Base.similar(u::Gaugefields_4D_GB300) =
     Gaugefields_4D_GB300(u.ctx, nothing, u.mu, u.NC, u.NX, u.NY, u.NZ, u.NT, u.NV)

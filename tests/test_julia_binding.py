@@ -114,3 +114,14 @@ def test_md_methods_are_typed_on_the_driver():
     assert len(re.findall(r"function md_force!\(", jl)) == 1
     # the backend is a positional selector: the reference's keyword method is not redefined
     assert re.search(r"function gauge_configuration\(lattice::NTuple\{4,<:Integer\}, backend::GB300Backend;", jl)
+
+
+def test_configuration_accessors_are_defined():
+    """measure_plaquette(U) and the accessors of src/API.jl:262-295 reach the
+    backend through size, gauge_backend and gauge_halo_width of a direction."""
+    jl = open(JL).read()
+    assert re.search(r"Base\.size\(u::Gaugefields_4D_GB300\) = \(u\.NC, u\.NC, u\.NX, u\.NY, u\.NZ, u\.NT\)", jl)
+    assert "Gaugefields.gauge_backend(u::Gaugefields_4D_GB300)" in jl
+    assert "Gaugefields.gauge_halo_width(::Gaugefields_4D_GB300)" in jl
+    assert re.search(r"function copy_configuration!\(destination::GB300Config, source::GB300Config\)", jl)
+
