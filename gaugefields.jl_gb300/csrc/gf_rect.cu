@@ -166,8 +166,9 @@ __global__ void __launch_bounds__(128) k_dsdu_rect(SRC U, typename LinkFull<R>::
 }
 
 // --------------------------------------------------------------------------
-// The same force in double-float arithmetic (the GF_DFLOAT form on thin
-// links), as a loop over a table of products with one inlined fixed-grid
+// The same force in double-float arithmetic (the GF_DFLOAT form: the force
+// on thin links, or dS/dUbar on a stack's top level), as a loop over a table
+// of products with one inlined fixed-grid
 // product (the double-float stencils overflow the instruction cache when
 // their products are inlined). Per plane (mu, nu): ops 0-3 add the two
 // plaquette staples to S (add_staple_pair), ops 4-27 the six rectangle
