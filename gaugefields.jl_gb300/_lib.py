@@ -108,6 +108,7 @@ SIGNATURES = {
     "gf_prof_read": [_P, _I, _DP, ctypes.POINTER(ctypes.c_longlong)],
     "gf_launch_count": [ctypes.POINTER(ctypes.c_longlong)],
     "gf_plaquette_noalloc": [_P, ctypes.POINTER(ctypes.c_int), _P, _P],
+    "gf_polyakov_loop": [_P, _P, _DP],
 }
 
 KERNEL_CLASSES = ["plaquette", "force", "link_update", "stout_fwd", "bwd_local", "bwd_gather", "stout_fwd64",

@@ -22,6 +22,7 @@ from ._lib import MDParams, call
 
 __all__ = [
     "GB300Backend", "gauge_configuration", "measure_plaquette", "calculate_Plaquette", "construct_staple_",
+    "calculate_Polyakov_loop", "measure_polyakov_loop",
     "gauge_momenta", "gaussian_momenta_", "gaussian_momenta", "GaugeAction", "push_", "evaluate_GaugeAction",
     "QPQ", "PQP", "OmelyanPQP", "md_driver", "md_step_size", "md_hamiltonian", "md_potential", "md_force_",
     "md_action_workspace", "update_gaugefields_", "update_momenta_", "md_step_", "md_trajectory_",
@@ -340,6 +341,21 @@ def calculate_Plaquette(U, temp=None, staple=None):
     out = ctypes.c_double()
     call("gf_plaquette", U.ctx.h, U.field.h, ctypes.byref(out), ctx=U.ctx.h)
     return out.value
+
+
+def calculate_Polyakov_loop(U, temp1=None, temp2=None):
+    """calculate_Polyakov_loop(U, temp1, temp2) (src/AbstractGaugefields.jl:
+    2929-2956): the mean over the first time slice of tr of the product of
+    the time links, a complex number; deterministic."""
+    out = (ctypes.c_double * 2)()
+    call("gf_polyakov_loop", U.ctx.h, U.field.h, out, ctx=U.ctx.h)
+    return complex(out[0], out[1])
+
+
+def measure_polyakov_loop(U, normalize=True):
+    """measure_polyakov_loop(U; normalize=true) (src/API.jl:412-417)."""
+    v = calculate_Polyakov_loop(U)
+    return v / U.NC if normalize else v
 
 
 def measure_plaquette(U, normalize=True):

@@ -348,6 +348,14 @@ extern "C" int gf_plaquette(gf_ctx* ctx, const gf_field* U, double* out) {
   *out = plaquette_sum(ctx, U);
   API_END(ctx)
 }
+extern "C" int gf_polyakov_loop(gf_ctx* ctx, const gf_field* U, double* out) {
+  API_BEGIN
+  need(ctx && U && out, "gf_polyakov_loop: null argument");
+  need_ctx(ctx, U);
+  need_kind(U, GF_LINK64, "gf_polyakov_loop: U");
+  polyakov_loop(ctx, U, out);
+  API_END(ctx)
+}
 extern "C" int gf_action(gf_ctx* ctx, const gf_field* U, double beta, double* out) {
   API_BEGIN
   need(ctx && U && out, "gf_action: null argument");

@@ -166,6 +166,8 @@ void mom_scale(gf_ctx* ctx, gf_field* y, double a);                      // y *=
 
 // ---- Wilson action pieces (gf_wilson.cu) ----
 double plaquette_sum(gf_ctx* ctx, const gf_field* U, bool df = false);  // sum_x sum_{mu<nu} Re tr P
+// mean over the t = 0 slice of tr prod_t U_T: out = {Re, Im}
+void polyakov_loop(gf_ctx* ctx, const gf_field* U, double out[2]);
 void staple_up(gf_ctx* ctx, const gf_field* U, int mu, gf_field* V);  // construct_staple! (mu field slot)
 // P <- keep * P + coef * TA-coefficients(U_mu * S_mu), S = sum of the six
 // staples (dS/dU order); keep = 0 overwrites P without reading it.

@@ -47,6 +47,38 @@ double plaquette_sum(gf_ctx* ctx, const gf_field* U, bool df) {
   return finish_reduction(ctx, nb);
 }
 
+// Polyakov loop (calculate_Polyakov_loop, src/AbstractGaugefields.jl:
+// 2929-2956): for each site x of the t = 0 slice, Re or Im (comp 0 / 1) of
+// tr(U_T(x, 0) U_T(x, 1) ... U_T(x, NT - 1)), one partial per block. One
+// thread per spatial site, the product along T in fp64.
+__global__ void __launch_bounds__(128) k_polyakov(Src64 U, Geom g, int comp, double* __restrict__ part) {
+  const int vs = g.stride[3];  // NX NY NZ
+  const int sp = blockIdx.x * blockDim.x + threadIdx.x;
+  double v = 0.0;
+  if (sp < vs) {
+    const int x = sp % g.L[0], r = sp / g.L[0];
+    const int par0 = (x + r % g.L[1] + r / g.L[1]) & 1;
+    mat3<double> p = U(3, eo_of_lex(g, sp, par0), g.vol);
+#pragma unroll 1
+    for (int t = 1; t < g.L[3]; ++t) p = mul_nn(p, U(3, eo_of_lex(g, sp + t * vs, par0 ^ (t & 1)), g.vol));
+    const cplx<double> tr = trace(p);
+    v = comp ? tr.im : tr.re;
+  }
+  block_partial_sum(v, part);
+}
+
+void polyakov_loop(gf_ctx* ctx, const gf_field* U, double out[2]) {
+  if (U->kind != GF_LINK64) throw gf_error(GF_EINVAL, "Polyakov loop: links must be LINK64");
+  const int vs = ctx->geom.stride[3];
+  const int nb = blocks_for(vs, 128);
+  ProfScope prof(ctx, GF_K_PLAQ);
+  for (int c = 0; c < 2; ++c) {
+    k_polyakov<<<nb, 128, 0, ctx->stream>>>(Src64{(const double2*)U->ptr}, ctx->geom, c, ctx->d_partials);
+    GF_CHECK_LAUNCH();
+    out[c] = finish_reduction(ctx, nb) / vs;
+  }
+}
+
 // construct_staple!: V_mu = sum_{nu != mu} U_nu(x) U_mu(x+nu) U_nu(x+mu)^dag = S_mu^dag
 __global__ void __launch_bounds__(128) k_staple_up(Src64 U, Geom g, int mu, double2* __restrict__ out) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;

@@ -152,6 +152,11 @@ int gf_reunitarize(gf_ctx* ctx, gf_field* U);
  * sum_mu Re tr(U_mu V_mu^dag)/2 = sum_x sum_{mu<nu} Re tr P_munu(x).
  * measure_plaquette divides by 6*V*3 (API.jl:395-404). Deterministic. */
 int gf_plaquette(gf_ctx* ctx, const gf_field* U, double* out);
+/* calculate_Polyakov_loop(U, temp1, temp2) (AbstractGaugefields.jl:
+ * 2929-2956): the mean over the sites of the t = 0 slice of
+ * tr(U_T(x,0) U_T(x,1) ... U_T(x,NT-1)); out[0] = Re, out[1] = Im.
+ * measure_polyakov_loop (API.jl:412-417) divides by 3. Deterministic. */
+int gf_polyakov_loop(gf_ctx* ctx, const gf_field* U, double* out);
 /* md_potential(::GaugeAction) (molecular_dynamics.jl:247) for the Wilson
  * action beta/2 * (plaq U plaq^dag): -(beta/3) sum Re tr P. */
 int gf_action(gf_ctx* ctx, const gf_field* U, double beta, double* out);

@@ -39,7 +39,7 @@ using Gaugefields
 import Gaugefields: md_action_workspace, md_potential, md_force!, md_hamiltonian, update_momenta!,
                     update_gaugefields!, md_trajectory!, md_step!, gauge_configuration, gaussian_momenta!,
                     calculate_Plaquette, substitute_U!, clear_U!, initialize_TA_Gaugefields, back_prop,
-                    copy_configuration!, copy_configuration
+                    copy_configuration!, copy_configuration, calculate_Polyakov_loop
 import Gaugefields.AbstractGaugefields_module: Gaugefields_4D, TA_Gaugefields_4D
 import Gaugefields.Abstractsmearing_module: CovLayer, apply_layer!, layer_pullback!, parameter_derivatives
 import Gaugefields.Gradientflow_module: Gradientflow, flow!
@@ -302,6 +302,21 @@ function calculate_Plaquette(U::GB300Config, temp=nothing, staple=nothing)
     check(ccall((:gf_plaquette, libgf), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ref{Cdouble}), ctx.h, config_field(U).h, out),
           ctx)
     return out[]
+end
+
+"""
+    calculate_Polyakov_loop(U::Vector{<:Gaugefields_4D_GB300}, temp1, temp2)
+
+`calculate_Polyakov_loop` (`src/AbstractGaugefields.jl:2929-2956`): the mean
+over the first time slice of tr of the product of the time links (complex);
+`measure_polyakov_loop` divides it by 3. Deterministic.
+"""
+function calculate_Polyakov_loop(U::GB300Config, temp1=nothing, temp2=nothing)
+    ctx = U[1].ctx
+    out = zeros(Cdouble, 2)
+    check(ccall((:gf_polyakov_loop, libgf), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cdouble}), ctx.h, config_field(U).h,
+                out), ctx)
+    return complex(out[1], out[2])
 end
 
 """

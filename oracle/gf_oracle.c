@@ -563,6 +563,34 @@ void or_staple(const int L[4], const cdbl* U, int mu, cdbl* Vout) {
 }
 
 /* calculate_Plaquette: real(sum_mu tr(U_mu V_mu^dag) * 0.5) */
+/* calculate_Polyakov_loop(U, temp1, temp2) (src/AbstractGaugefields.jl:
+ * 2929-2956): the products U_T(x) U_T(x+T) ... U_T(x+(NT-1)T) from the
+ * sites of the first time slice, traced and averaged over that slice
+ * (partial_tr over the slice / NX NY NZ); out = {Re, Im} */
+void or_polyakov_loop(const int L[4], const cdbl* U, double out[2]) {
+  Lat lat = mklat(L);
+  const long vs = (long)L[0] * L[1] * L[2];
+  double* pr = (double*)calloc((size_t)vs, sizeof(double));
+  double* pi = (double*)calloc((size_t)vs, sizeof(double));
+#pragma omp parallel for schedule(static)
+  for (long s = 0; s < vs; ++s) {
+    long x = s;  /* lexicographic index of (x, y, z, t = 0) */
+    M3 p = ld(U, &lat, 3, x);
+    for (int t = 1; t < L[3]; ++t) {
+      x = shift1(&lat, x, 3, 1);
+      M3 u = ld(U, &lat, 3, x);
+      p = mmul(&p, &u);
+    }
+    cdbl tr = mtr(&p);
+    pr[s] = creal(tr);
+    pi[s] = cimag(tr);
+  }
+  out[0] = sum_accurate(pr, vs) / (double)vs;
+  out[1] = sum_accurate(pi, vs) / (double)vs;
+  free(pr);
+  free(pi);
+}
+
 double or_plaquette(const int L[4], const cdbl* U) {
   Lat lat = mklat(L);
   double* part = (double*)calloc((size_t)lat.V, sizeof(double));

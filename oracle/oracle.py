@@ -80,6 +80,7 @@ def _declare(l):
         "or_loop_trace": ([_P, _P, _I], _D),
         "or_action_loops": ([_P, _P, _D, _D], _D),
         "or_force_loops": ([_P, _P, _D, _D, _P], None),
+        "or_polyakov_loop": ([_P, _P, _P], None),
         "or_stout_force_loops": ([_P, _P, _I, _P, _D, _D, _P], None),
         "or_stout_action_loops": ([_P, _P, _I, _P, _D, _D], _D),
         "or_loop_staple_count": ([_I, _I], _I),
@@ -175,6 +176,15 @@ def gauss_mom(L, seed, sweep=0):
 def plaquette(L, U):
     _chk(U, np.complex128)
     return lib().or_plaquette(_ptr(_L(L)), _ptr(U))
+
+
+def polyakov_loop(L, U):
+    """calculate_Polyakov_loop: mean over the first time slice of the traced
+    product of the time links (complex)."""
+    _chk(U, np.complex128)
+    out = np.zeros(2)
+    lib().or_polyakov_loop(_ptr(_L(L)), _ptr(U), _ptr(out))
+    return complex(out[0], out[1])
 
 
 def staple(L, U, mu):

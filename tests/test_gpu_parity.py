@@ -95,6 +95,18 @@ def test_plaquette_and_action(pkg, oracle, hot8):
     assert abs(v - vr) <= 1e-13 * abs(vr)
 
 
+@pytest.mark.parametrize("L", [(4, 4, 4, 6), (6, 4, 8, 8)])
+def test_polyakov_loop(pkg, oracle, L):
+    """calculate_Polyakov_loop / measure_polyakov_loop against the oracle
+    (complex, 1e-13), and 1 on a cold start (test/high_level_api.jl:49)."""
+    U = pkg.gauge_configuration(L, start="hot", seed=73)
+    ref = oracle.polyakov_loop(list(L), U.to_host())
+    got = pkg.calculate_Polyakov_loop(U)
+    assert abs(got - ref) < 1e-13
+    assert abs(pkg.measure_polyakov_loop(U) - ref / 3) < 1e-13
+    assert pkg.measure_polyakov_loop(pkg.gauge_configuration(L, start="cold")) == 1
+
+
 def test_plaquette_is_deterministic(pkg, hot8):
     a = pkg.calculate_Plaquette(hot8)
     b = pkg.calculate_Plaquette(hot8)

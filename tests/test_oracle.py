@@ -186,6 +186,29 @@ def test_plaquette_gauge_invariance(oracle):
                                                                         rel=1e-12)
 
 
+def test_polyakov_loop_invariants(oracle):
+    """calculate_Polyakov_loop: 3 on a cold start (measure_polyakov_loop == 1,
+    test/high_level_api.jl:49), gauge invariant, and multiplied by the centre
+    element exp(2 pi i / 3) when every time link of one time slice is."""
+    L = [4, 4, 4, 6]
+    V = 4 * 4 * 4 * 6
+    assert oracle.polyakov_loop(L, oracle.cold_start(L)) == 3
+    U = oracle.hot_start(L, 23)
+    p0 = oracle.polyakov_loop(L, U)
+    G = oracle.mats(oracle.hot_start(L, 24))[0]
+    M = oracle.mats(U)
+    Mt = np.empty_like(M)
+    for mu in range(4):
+        nb = np.array([oracle_shift(L, x, mu) for x in range(V)])
+        Mt[mu] = G @ M[mu] @ np.conj(np.swapaxes(G[nb], -1, -2))
+    assert abs(oracle.polyakov_loop(L, oracle.from_mats(Mt)) - p0) < 1e-13
+    z = np.exp(2j * np.pi / 3)
+    Mz = M.copy()
+    t2 = np.arange(V) // 64 == 2  # the time slice t = 2
+    Mz[3, t2] *= z
+    assert abs(oracle.polyakov_loop(L, oracle.from_mats(Mz)) - z * p0) < 1e-13
+
+
 def oracle_shift(L, lex, mu):
     x = [lex % L[0], (lex // L[0]) % L[1], (lex // (L[0] * L[1])) % L[2], lex // (L[0] * L[1] * L[2])]
     x[mu] = (x[mu] + 1) % L[mu]
