@@ -564,6 +564,7 @@ def run_wilson_mode(args):
     # the staple/force kernel reads U (4 x 144 B) and P (4 x 64 B) and writes P per site
     force_bytes = 4 * V * (144 + 64 + 64)
     plaq = pkg.measure_plaquette(U)
+    Udf = pkg.copy_configuration(U)
     g = pkg.Gradientflow(U, Nflow=1, eps=0.01)
     E = []
     torch.cuda.synchronize()
@@ -572,12 +573,23 @@ def run_wilson_mode(args):
         pkg.flow_(U, g)
         E.append(36.0 * (1.0 - pkg.measure_plaquette(U)))
     flow_sec = time.perf_counter() - t0
+    # the same flow in the double-float form, from the same configuration
+    gdf = pkg.Gradientflow(Udf, Nflow=1, eps=0.01, precision="dfloat")
+    Edf = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(200):
+        pkg.flow_(Udf, gdf)
+        Edf.append(36.0 * (1.0 - pkg.measure_plaquette(Udf)))
+    flow_df_sec = time.perf_counter() - t0
     link_updates = 4 * V * (NSTEPS + 1) * args.steps
     out = {"mode": "wilson", "lattice": [L] * 4, "workload": "%d^4 cold start, fp64 Wilson HMC beta=6.0, tau=1, "
            "20 QPQ steps; RK3 flow eps=0.01 to t=2" % L, "trajectories": args.steps, "traj_per_s": args.steps / sec,
            "link_updates_per_s": link_updates / sec, "accepted": acc, "plaquette": plaq,
            "force_kernel": {"avg_ms": force_ms, "algorithmic_GBps": force_bytes / force_ms / 1e6},
            "flow_steps_per_s": 200 / flow_sec, "E_t": [[round(0.01 * (k + 1), 2), E[k]] for k in range(0, 200, 20)],
+           "flow_dfloat": {"steps_per_s": 200 / flow_df_sec,
+                           "max_rel_E_diff": max(abs(a - b) / abs(b) for a, b in zip(Edf, E))},
            "t2E_at_t2": 4.0 * E[-1]}
     print(json.dumps(out))
     return 0

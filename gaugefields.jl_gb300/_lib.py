@@ -102,6 +102,7 @@ SIGNATURES = {
     "gf_stout_param_derivatives": [_P, _P, _P, _P, _P],
     "gf_field_axpy": [_P, _P, _D, _P],
     "gf_flow": [_P, _P, _D, _I],
+    "gf_flow_precision": [_P, _P, _D, _I, _I],
     "gf_flow_loops": [_P, _P, _D, _I, _D, _D],
     "gf_flow_force": [_P, _P, _P, _D],
     "gf_prof_enable": [_P, _I],

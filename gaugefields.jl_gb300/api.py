@@ -955,11 +955,17 @@ def get_parameter_derivatives(dSdUbar, smearing, U, precision="fp64"):
 # gradient flow (src/smearing/gradientflow.jl)
 # ---------------------------------------------------------------------------
 class Gradientflow:
-    """Wilson flow with the Luescher RK3 integrator (gradientflow.jl:118-161)."""
+    """Wilson flow with the Luescher RK3 integrator (gradientflow.jl:118-161).
+    precision: "fp64" (the reference's arithmetic) or "dfloat" (the force and
+    the exponentials in double-float arithmetic on the fp32 pipes, fp64
+    fields)."""
 
-    def __init__(self, U, Nflow=1, eps=0.01):
+    def __init__(self, U, Nflow=1, eps=0.01, precision="fp64"):
+        if precision not in ("fp64", "dfloat"):
+            raise ValueError("the flow's precision must be 'fp64' or 'dfloat'")
         self.Nflow = int(Nflow)
         self.eps = float(eps)
+        self.precision = precision
 
 
 class Gradientflow_general:
@@ -1008,7 +1014,8 @@ def flow_(U, g):
         call("gf_flow_loops", U.ctx.h, U.field.h, ctypes.c_double(g.eps), int(g.Nflow), ctypes.c_double(g.c_plaq),
              ctypes.c_double(g.c_rect), ctx=U.ctx.h)
         return U
-    call("gf_flow", U.ctx.h, U.field.h, ctypes.c_double(g.eps), int(g.Nflow), ctx=U.ctx.h)
+    call("gf_flow_precision", U.ctx.h, U.field.h, ctypes.c_double(g.eps), int(g.Nflow), _PRECISION[g.precision],
+         ctx=U.ctx.h)
     return U
 
 

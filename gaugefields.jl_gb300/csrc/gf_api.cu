@@ -866,13 +866,10 @@ extern "C" int gf_flow_force(gf_ctx* ctx, const gf_field* U, gf_field* F, double
   API_END(ctx)
 }
 
-extern "C" int gf_flow(gf_ctx* ctx, gf_field* U, double eps, int nsteps) {
-  API_BEGIN
-  need(ctx && U, "gf_flow: null argument");
-  need_ctx(ctx, U);
-  need_kind(U, GF_LINK64, "gf_flow: U");
-  need(std::isfinite(eps) && eps != 0.0, "gf_flow: eps must be finite and nonzero");
-  need(nsteps >= 0, "gf_flow: nsteps must be nonnegative");
+// RK3 Wilson-flow steps (flow!, src/smearing/gradientflow.jl:171-238) in fp64
+// or, df, with the force and the exponentials in double-float arithmetic on
+// the fp64 fields
+static void flow_steps(gf_ctx* ctx, gf_field* U, double eps, int nsteps, bool df) {
   if (!ctx->w_link64) ctx->w_link64 = field_new(ctx, GF_LINK64);
   if (!ctx->w_link64b) ctx->w_link64b = field_new(ctx, GF_LINK64);
   if (!ctx->w_mom[0]) ctx->w_mom[0] = field_new(ctx, GF_MOM64);
@@ -881,13 +878,28 @@ extern "C" int gf_flow(gf_ctx* ctx, gf_field* U, double eps, int nsteps) {
   gf_field* G = ctx->w_mom[0];
   const double c0 = 17.0 * eps / 36.0;
   for (int n = 0; n < nsteps; ++n) {
-    flow_force(ctx, U, G, c0, 0.0);                 // G = 17eps/36 F0
-    exp_mom_links(ctx, W1, G, -9.0 / 17.0, U);      // W1 = exp(-eps/4 F0) U
-    flow_force(ctx, W1, G, -8.0 * eps / 9.0, 1.0);  // G = 17eps/36 F0 - 8eps/9 F1
-    exp_mom_links(ctx, W2, G, 1.0, W1);             // W2 = exp(G) W1
-    flow_force(ctx, W2, G, -0.75 * eps, -1.0);      // G = -G - 3eps/4 F2
-    exp_mom_links(ctx, U, G, 1.0, W2);              // U = exp(G) W2
+    flow_force(ctx, U, G, c0, 0.0, df);                 // G = 17eps/36 F0
+    exp_mom_links(ctx, W1, G, -9.0 / 17.0, U, df);      // W1 = exp(-eps/4 F0) U
+    flow_force(ctx, W1, G, -8.0 * eps / 9.0, 1.0, df);  // G = 17eps/36 F0 - 8eps/9 F1
+    exp_mom_links(ctx, W2, G, 1.0, W1, df);             // W2 = exp(G) W1
+    flow_force(ctx, W2, G, -0.75 * eps, -1.0, df);      // G = -G - 3eps/4 F2
+    exp_mom_links(ctx, U, G, 1.0, W2, df);              // U = exp(G) W2
   }
+}
+
+extern "C" int gf_flow(gf_ctx* ctx, gf_field* U, double eps, int nsteps) {
+  return gf_flow_precision(ctx, U, eps, nsteps, GF_FP64);
+}
+
+extern "C" int gf_flow_precision(gf_ctx* ctx, gf_field* U, double eps, int nsteps, int precision) {
+  API_BEGIN
+  need(ctx && U, "gf_flow: null argument");
+  need_ctx(ctx, U);
+  need_kind(U, GF_LINK64, "gf_flow: U");
+  need(std::isfinite(eps) && eps != 0.0, "gf_flow: eps must be finite and nonzero");
+  need(nsteps >= 0, "gf_flow: nsteps must be nonnegative");
+  need(precision == GF_FP64 || precision == GF_DFLOAT, "gf_flow: precision must be GF_FP64 or GF_DFLOAT");
+  flow_steps(ctx, U, eps, nsteps, precision == GF_DFLOAT);
   API_END(ctx)
 }
 

@@ -182,13 +182,17 @@ void loops_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double cp, do
 // D = cp S + cr R (plaquette and rectangle staples) on a stack's top level:
 // LINK64 -> MAT64, LINK32 -> MAT32, LINKDF -> MATDF (double-float)
 void loops_dsdu(gf_ctx* ctx, const gf_field* Ubar, gf_field* D, double cp, double cr);
+// P <- keep P + coef c(U S), S the six plaquette staples, as a double-float
+// table loop of fixed-grid products on a double-float-native copy of U
+void plaquette_force_df(gf_ctx* ctx, const gf_field* U, gf_field* P, double coef, double keep);
 
 // ---- link update (gf_update.cu) ----
 // U <- exp(i eps P) U, optional re-unitarisation, optional fp32 shadow copy.
 // df: double-float arithmetic on the fp32 pipes (the mixed form), else fp64.
 void link_update(gf_ctx* ctx, gf_field* U, const gf_field* P, double eps, int reunit, gf_field* shadow32,
                  bool df = false);
-void exp_mom_links(gf_ctx* ctx, gf_field* W, const gf_field* P, double a, const gf_field* U);  // W = exp(i a P) U
+// W = exp(i a P) U (fp64, or double-float arithmetic on the fp64 fields)
+void exp_mom_links(gf_ctx* ctx, gf_field* W, const gf_field* P, double a, const gf_field* U, bool df = false);
 void reunitarize_links(gf_ctx* ctx, gf_field* U);
 void link64_to_32(gf_ctx* ctx, gf_field* dst, const gf_field* src);
 
@@ -206,6 +210,6 @@ const gf_field* stout_top(const gf_stout* st);
 // ---- flow (gf_flow.cu) ----
 // F <- keep * F + factor * TA-coefficients(U_mu V_mu^dag), V = six-staple sum
 // (add_force!, plaqonly)
-void flow_force(gf_ctx* ctx, const gf_field* U, gf_field* F, double factor, double keep);
+void flow_force(gf_ctx* ctx, const gf_field* U, gf_field* F, double factor, double keep, bool df = false);
 
 }  // namespace gf

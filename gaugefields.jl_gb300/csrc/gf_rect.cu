@@ -221,8 +221,9 @@ __device__ __forceinline__ mat3<dfl> rect_operand(int src, int dir, int mo, int 
 // P_mu(x) <- keep * P_mu(x) + c(U_mu(x) (cp S_mu(x) + cr R_mu(x))) as
 // k_force_rect, the staples, the combination and the projection in
 // double-float, on double-float-native links; DSDU: D_mu(x) = cp S + cr R
-// (as k_dsdu_rect, double-float-native) instead
-template <bool DSDU>
+// (as k_dsdu_rect, double-float-native) instead. NOPS = 4 runs only the
+// plaquette staples (the Wilson force; R stays zero).
+template <bool DSDU, int NOPS>
 __global__ void __launch_bounds__(128, 3)
     k_force_rect_df(const float4* __restrict__ U, double* __restrict__ P, float4* __restrict__ D, Geom g, dfl cp,
                     dfl cr, double keep) {
@@ -238,7 +239,7 @@ __global__ void __launch_bounds__(128, 3)
   for (int k = 1; k < 4; ++k) {
     const int nu = (mu + k) & 3;
 #pragma unroll 1
-    for (int q = 0; q < 28; ++q) {
+    for (int q = 0; q < NOPS; ++q) {
       const DfOpR op = c_rect_ops[q];
       const mat3<dfl> A = rect_operand(op.a_src, op.a_dir, op.a_mo, op.a_no, op.a_dag, sm, tid, U, g, st, mu, nu);
       const mat3<dfl> B = rect_operand(op.b_src, op.b_dir, op.b_mo, op.b_no, op.b_dag, sm, tid, U, g, st, mu, nu);
@@ -272,9 +273,10 @@ __global__ void __launch_bounds__(128, 3)
   }
 }
 
-static void rect_df(gf_ctx* ctx, const float4* U, gf_field* P, gf_field* D, double cp, double cr, double keep) {
+static void rect_df(gf_ctx* ctx, const float4* U, gf_field* P, gf_field* D, double cp, double cr, double keep,
+                    bool plaquette_only = false) {
   const size_t smem = (size_t)GF_RECT_SLOTS * 36 * 128 * sizeof(float);
-  auto kern = D ? k_force_rect_df<true> : k_force_rect_df<false>;
+  auto kern = plaquette_only ? k_force_rect_df<false, 4> : (D ? k_force_rect_df<true, 28> : k_force_rect_df<false, 28>);
   GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid = stencil_grid(ctx->geom.vol, 128);
   ProfScope prof(ctx, GF_K_RECT_DF);
@@ -322,6 +324,14 @@ void loops_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double cp, do
     throw gf_error(GF_EINVAL, "force: the rectangle force takes LINK64 or LINK32 links");
   }
   GF_CHECK_LAUNCH();
+}
+
+void plaquette_force_df(gf_ctx* ctx, const gf_field* U, gf_field* P, double coef, double keep) {
+  if (P->kind != GF_MOM64) throw gf_error(GF_EINVAL, "force: output must be MOM64");
+  if (U->kind != GF_LINK64) throw gf_error(GF_EINVAL, "force: the double-float force takes LINK64 links");
+  if (!ctx->w_linkdf) ctx->w_linkdf = field_new(ctx, GF_LINKDF);
+  copy_field(ctx, ctx->w_linkdf, U);
+  rect_df(ctx, (const float4*)ctx->w_linkdf->ptr, P, nullptr, coef, 0.0, keep, true);
 }
 
 void loops_dsdu(gf_ctx* ctx, const gf_field* Ubar, gf_field* D, double cp, double cr) {

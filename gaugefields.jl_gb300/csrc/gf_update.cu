@@ -67,10 +67,14 @@ void link_update(gf_ctx* ctx, gf_field* U, const gf_field* P, double eps, int re
 
 // exp_aF_U!(W, a, F, U) (src/AbstractGaugefields.jl:2810-2842): W_mu = exp(a F_mu) U_mu
 // with F in su(3) coefficients, i.e. exp(i a sum_a F_a lambda_a / 2) U.
-void exp_mom_links(gf_ctx* ctx, gf_field* W, const gf_field* P, double a, const gf_field* U) {
+void exp_mom_links(gf_ctx* ctx, gf_field* W, const gf_field* P, double a, const gf_field* U, bool df) {
   dim3 grid(blocks_for(ctx->geom.vol, 128), 4);
-  ProfScope prof(ctx, GF_K_LINK_UPDATE);
-  k_link_update<double><<<grid, 128, 0, ctx->stream>>>((const double2*)U->ptr, (double2*)W->ptr,
+  ProfScope prof(ctx, df ? GF_K_LINK_UPDATE_DF : GF_K_LINK_UPDATE);
+  if (df)
+    k_link_update<dfl><<<grid, 128, 0, ctx->stream>>>((const double2*)U->ptr, (double2*)W->ptr,
+                                                      (const double*)P->ptr, ctx->geom, dfl(a), 0, nullptr);
+  else
+    k_link_update<double><<<grid, 128, 0, ctx->stream>>>((const double2*)U->ptr, (double2*)W->ptr,
                                                          (const double*)P->ptr, ctx->geom, a, 0, nullptr);
   GF_CHECK_LAUNCH();
 }

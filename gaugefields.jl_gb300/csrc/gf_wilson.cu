@@ -157,8 +157,11 @@ void wilson_force_coef(gf_ctx* ctx, const gf_field* U, gf_field* P, double coef,
 }
 
 // add_force!(F, U; plaqonly=true): F += factor * TA(U_mu V_mu^dag), V^dag = S
-void flow_force(gf_ctx* ctx, const gf_field* U, gf_field* F, double factor, double keep) {
-  wilson_force_coef(ctx, U, F, factor, keep);
+// the flow's force; double-float: the plaquette-staple table kernel of
+// gf_rect.cu (fixed-grid products, 2.4x the inlined double-float force)
+void flow_force(gf_ctx* ctx, const gf_field* U, gf_field* F, double factor, double keep, bool df) {
+  if (df) plaquette_force_df(ctx, U, F, factor, keep);
+  else wilson_force_coef(ctx, U, F, factor, keep);
 }
 
 }  // namespace gf

@@ -244,6 +244,10 @@ int gf_stout_mom_update(gf_ctx* ctx, gf_stout* st, gf_field* P, const gf_field* 
 /* flow!(U, ::Gradientflow) (smearing/gradientflow.jl:171-238): nsteps RK3
  * Wilson-flow steps of size eps. */
 int gf_flow(gf_ctx* ctx, gf_field* U, double eps, int nsteps);
+/* The same flow with the force and the exponentials in double-float
+ * arithmetic on the fp32 pipes (precision GF_DFLOAT; the fields stay fp64)
+ * or in fp64 (GF_FP64, = gf_flow). */
+int gf_flow_precision(gf_ctx* ctx, gf_field* U, double eps, int nsteps, int precision);
 /* flow!(U, ::Gradientflow_general) (smearing/gradientflow.jl:240-336) for the
  * action with the plaquette loops at c_plaq and the rectangle loops at c_rect
  * (gradient_flow(U, [:plaquette, :rectangular], [c_plaq, c_rect]), API.jl:

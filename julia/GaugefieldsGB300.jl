@@ -550,10 +550,13 @@ end
 # ---------------------------------------------------------------------------
 # gradient flow (src/smearing/gradientflow.jl:171-238)
 # ---------------------------------------------------------------------------
-function flow!(U::GB300Config, g::Gradientflow)
+# precision = GF_DFLOAT runs the force and the exponentials in double-float
+# arithmetic on the fp32 pipes (the fields stay fp64); GF_FP64 is the
+# reference's arithmetic
+function flow!(U::GB300Config, g::Gradientflow; precision::Integer=GF_FP64)
     ctx = U[1].ctx
-    check(ccall((:gf_flow, libgf), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cdouble, Cint), ctx.h, config_field(U).h,
-                g.eps, g.Nflow), ctx)
+    check(ccall((:gf_flow_precision, libgf), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cdouble, Cint, Cint), ctx.h,
+                config_field(U).h, g.eps, g.Nflow, precision), ctx)
     return U
 end
 

@@ -191,3 +191,24 @@ def test_partial_blocks_in_every_form(pkg, oracle, exact_exp_oracle):
     h = exact_exp_oracle.md_trajectory(list(L), Uh, Ph, 6.0, 0.3, 3, rho=[0.1])
     assert abs(res.delta_hamiltonian - h[2]) <= 1e-10
     assert frob_links(U.to_host(), Uh) < 1e-12
+
+
+def test_dfloat_flow_tracks_fp64(pkg, oracle):
+    """The RK3 Wilson flow with the force and the exponentials in double-float
+    (gf_flow_precision, GF_DFLOAT): 10 steps of eps = 0.02 from an 8^4 Haar
+    start equal the fp64 flow's links to 1e-12 and the oracle's to 1e-11;
+    the plaquette to 1e-13 relative."""
+    U = pkg.gauge_configuration(L8, start="hot", seed=81)
+    Uh = U.to_host()
+    V = pkg.copy_configuration(U)
+    pkg.flow_(U, pkg.Gradientflow(U, Nflow=10, eps=0.02))
+    pkg.flow_(V, pkg.Gradientflow(V, Nflow=10, eps=0.02, precision="dfloat"))
+    oracle.flow(list(L8), Uh, 0.02, 10)
+    a, b = U.to_host(), V.to_host()
+    du, do = np.abs(b - a).max(), np.abs(b - Uh).max()
+    pa, pb = pkg.calculate_Plaquette(U), pkg.calculate_Plaquette(V)
+    print("dfloat flow: |dU| fp64 %.2e oracle %.2e  plaquette rel %.2e" % (du, do, abs(pb - pa) / abs(pa)))
+    assert du < 1e-12 and do < 1e-11 and abs(pb - pa) <= 1e-13 * abs(pa)
+    with pytest.raises(ValueError):
+        pkg.Gradientflow(U, precision="mixed")
+
