@@ -672,15 +672,23 @@ def run_scale_mode(args):
     r64 = pkg.md_trajectory_(U, P, drv)
     out["fp64"] = {"dH_first": r64.delta_hamiltonian, "trajectory_s": time.perf_counter() - t0}
     out["abs_dH_diff"] = abs(out["store"]["dH_first"] - r64.delta_hamiltonian)
-    # RK3 Wilson flow to t = 3 on the configuration after that trajectory
-    g = pkg.Gradientflow(U, Nflow=1, eps=0.01)
-    E = []
-    t0 = time.perf_counter()
-    for k in range(300):
-        pkg.flow_(U, g)
-        if (k + 1) % 25 == 0:
-            E.append([round(0.01 * (k + 1), 2), 36.0 * (1.0 - pkg.measure_plaquette(U))])
-    out["flow"] = {"steps": 300, "seconds": time.perf_counter() - t0, "E_t": E}
+    # RK3 Wilson flow to t = 3 on the configuration after that trajectory:
+    # fp64, and with --precision dfloat also the double-float flow from the
+    # same configuration
+    forms = ("fp64", "dfloat") if args.precision == "dfloat" else ("fp64",)
+    U0f = U.to_host() if len(forms) > 1 else None
+    for form in forms:
+        if form != "fp64":
+            U.from_host(U0f)
+        g = pkg.Gradientflow(U, Nflow=1, eps=0.01, precision=form)
+        E = []
+        t0 = time.perf_counter()
+        for k in range(300):
+            pkg.flow_(U, g)
+            if (k + 1) % 25 == 0:
+                E.append([round(0.01 * (k + 1), 2), 36.0 * (1.0 - pkg.measure_plaquette(U))])
+        out["flow" if form == "fp64" else "flow_dfloat"] = {"steps": 300, "seconds": time.perf_counter() - t0,
+                                                           "E_t": E}
     print(json.dumps(out))
     return 0
 
