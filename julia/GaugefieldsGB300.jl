@@ -39,12 +39,14 @@ using Gaugefields
 import Gaugefields: md_action_workspace, md_potential, md_force!, md_hamiltonian, update_momenta!,
                     update_gaugefields!, md_trajectory!, md_step!, gauge_configuration, gaussian_momenta!,
                     calculate_Plaquette, substitute_U!, clear_U!, initialize_TA_Gaugefields, back_prop,
-                    copy_configuration!, copy_configuration, calculate_Polyakov_loop
+                    copy_configuration!, copy_configuration, calculate_Polyakov_loop, save_configuration,
+                    load_configuration!
 import Gaugefields.AbstractGaugefields_module: Gaugefields_4D, TA_Gaugefields_4D
 import Gaugefields.Abstractsmearing_module: CovLayer, apply_layer!, layer_pullback!, parameter_derivatives
 import Gaugefields.Gradientflow_module: Gradientflow, flow!
 
-export GB300Backend, Gaugefields_4D_GB300, TA_Gaugefields_4D_GB300, StoutWilsonAction_GB300,
+export GB300Backend, Gaugefields_4D_GB300, TA_Gaugefields_4D_GB300, StoutWilsonAction_GB300, host_configuration,
+       upload_host!,
        STOUT_Layer_GB300, smear_gb300, GF_FP64, GF_MIXED, GF_DFLOAT
 
 const libgf = get(ENV, "GF_GB300_LIB", joinpath(@__DIR__, "..", "gaugefields.jl_gb300", "libgfgb300.so"))
@@ -337,6 +339,56 @@ function upload!(U::GB300Config, A::Array{ComplexF64})
     size(A) == (3, 3, ctx.L..., 4) || throw(ArgumentError("expected an array of size $((3, 3, ctx.L..., 4))"))
     GC.@preserve A check(ccall((:gf_upload_links, libgf), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{ComplexF64}), ctx.h,
                                 config_field(U).h, A), ctx)
+    return U
+end
+
+# ---------------------------------------------------------------------------
+# configuration files through the reference's own readers and writers
+# ---------------------------------------------------------------------------
+"""
+    host_configuration(U::Vector{<:Gaugefields_4D_GB300}) -> host configuration
+
+The configuration as the reference's own host fields (`LegacyBackend`,
+`src/API.jl:178-251`), one download: for the reference's configuration
+writers and any host-side analysis. `upload_host!(U, H)` copies host fields
+back.
+"""
+function host_configuration(U::GB300Config)
+    A = download(U)
+    NX, NY, NZ, NT = U[1].ctx.L
+    H = gauge_configuration((NX, NY, NZ, NT); backend=Gaugefields.LegacyBackend(), start=:cold)
+    for mu in 1:4, it in 1:NT, iz in 1:NZ, iy in 1:NY, ix in 1:NX, b in 1:3, a in 1:3
+        H[mu][a, b, ix, iy, iz, it] = A[a, b, ix, iy, iz, it, mu]
+    end
+    Gaugefields.set_wing_U!(H)
+    return H
+end
+
+function upload_host!(U::GB300Config, H)
+    NX, NY, NZ, NT = U[1].ctx.L
+    length(H) == 4 || throw(ArgumentError("the host configuration has length $(length(H)); expected 4"))
+    A = Array{ComplexF64}(undef, 3, 3, NX, NY, NZ, NT, 4)
+    for mu in 1:4, it in 1:NT, iz in 1:NZ, iy in 1:NY, ix in 1:NX, b in 1:3, a in 1:3
+        A[a, b, ix, iy, iz, it, mu] = H[mu][a, b, ix, iy, iz, it]
+    end
+    return upload!(U, A)
+end
+
+"""
+    save_configuration(filename, U::Vector{<:Gaugefields_4D_GB300}; format=:jld2, kwargs...)
+    load_configuration!(U::Vector{<:Gaugefields_4D_GB300}, filename; format=:jld2)
+
+`save_configuration` / `load_configuration!` (`src/API.jl:711-826`) for
+device configurations: the reference's own writers and readers (portable
+JLD2, ILDG, Bridge++) run on a host copy (`host_configuration`), so the files
+are the reference's byte for byte.
+"""
+save_configuration(filename, U::GB300Config; kwargs...) = save_configuration(filename, host_configuration(U); kwargs...)
+
+function load_configuration!(U::GB300Config, filename; format::Symbol=:jld2)
+    H = host_configuration(U)
+    load_configuration!(H, filename; format)
+    upload_host!(U, H)
     return U
 end
 

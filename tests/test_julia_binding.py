@@ -125,3 +125,14 @@ def test_configuration_accessors_are_defined():
     assert "Gaugefields.gauge_halo_width(::Gaugefields_4D_GB300)" in jl
     assert re.search(r"function copy_configuration!\(destination::GB300Config, source::GB300Config\)", jl)
 
+
+def test_configuration_files_go_through_the_reference_writers():
+    """save_configuration / load_configuration! of a device configuration run
+    the reference's own readers and writers (portable JLD2, ILDG, Bridge++) on
+    a LegacyBackend host copy (src/API.jl:711-826)."""
+    jl = open(JL).read()
+    assert re.search(r"save_configuration\(filename, U::GB300Config; kwargs\.\.\.\) =\s*save_configuration\(filename, "
+                     r"host_configuration\(U\); kwargs\.\.\.\)", jl)
+    assert re.search(r"function load_configuration!\(U::GB300Config, filename; format::Symbol=:jld2\)", jl)
+    assert "backend=Gaugefields.LegacyBackend()" in jl
+
