@@ -200,6 +200,9 @@ end
 Base.size(u::Gaugefields_4D_GB300) = (u.NC, u.NC, u.NX, u.NY, u.NZ, u.NT)
 Gaugefields.gauge_backend(u::Gaugefields_4D_GB300) = GB300Backend(u.ctx.device)
 Gaugefields.gauge_halo_width(::Gaugefields_4D_GB300) = 0
+# no halo to refresh (set_wing_U!, src/AbstractGaugefields.jl): a no-op
+Gaugefields.set_wing_U!(::Gaugefields_4D_GB300) = nothing
+Gaugefields.set_wing_U!(::GB300Config) = nothing
 
 Base.similar(u::Gaugefields_4D_GB300) =
     Gaugefields_4D_GB300(u.ctx, nothing, u.mu, u.NC, u.NX, u.NY, u.NZ, u.NT, u.NV)
