@@ -18,6 +18,7 @@
  *   STOUT forward!/backward + CdexpQdQ!     src/smearing/stout_fast.jl:250-408, 603-785, 888-946, 1031-1081
  *   STOUT_dataset (Cμ, dCμ/dUν lists)       src/smearing/stout_dataset.jl:10-80
  *   plaquette / rectangle loop sets         src/autostaples/wilsonloops.jl:233-330 (make_plaq, make_rect)
+ *   calculate_Polyakov_loop                 src/AbstractGaugefields.jl:2929-2956
  *   flow! (RK3), add_force!, exp_aF_U!      src/smearing/gradientflow.jl:171-238,
  *                                           src/AbstractGaugefields.jl:2717-2842
  * The Wilson-loop path lists come from the external package Wilsonloop.jl
