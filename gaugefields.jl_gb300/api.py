@@ -994,17 +994,20 @@ class Gradientflow_general:
         self.eps = float(eps)
 
 
-def gradient_flow(U, loops=None, coefficients=None, steps=1, step_size=0.01):
+def gradient_flow(U, loops=None, coefficients=None, steps=1, step_size=0.01, precision="fp64"):
     """gradient_flow(U; steps, step_size) and gradient_flow(U, loops,
-    coefficients; steps, step_size) (src/API.jl:420-438)."""
+    coefficients; steps, step_size) (src/API.jl:420-438); precision "dfloat"
+    selects the double-float Wilson flow (plaquette action only)."""
     if steps <= 0:
         raise ValueError("steps must be positive; got %d" % steps)
     if step_size <= 0:
         raise ValueError("step_size must be positive; got %s" % step_size)
     if loops is None and coefficients is None:
-        return Gradientflow(U, Nflow=steps, eps=step_size)
+        return Gradientflow(U, Nflow=steps, eps=step_size, precision=precision)
     if loops is None or coefficients is None:
         raise ValueError("a general-action flow needs both loops and coefficients")
+    if precision != "fp64":
+        raise ValueError("the general-action flow runs in fp64")
     return Gradientflow_general(U, loops, coefficients, Nflow=steps, eps=step_size)
 
 
