@@ -823,6 +823,13 @@ static void loops_dsdu(const Lat* lat, const cdbl* U, double c_plaq, double c_re
   }
 }
 
+/* dS/dU_mu(x) of the plaquette + rectangle action for every link, in the
+ * links' layout (exported for the tests of the device's staple tables) */
+void or_dsdu_loops(const int L[4], const cdbl* U, double c_plaq, double c_rect, cdbl* D) {
+  Lat lat = mklat(L);
+  loops_dsdu(&lat, U, c_plaq, c_rect, D);
+}
+
 /* F_mu (+)= factor * TA-coefficients of U_mu dS/dU_mu; accumulate = 0
  * overwrites F. */
 static void loops_force(const int L[4], const cdbl* U, double c_plaq, double c_rect, double factor, int accumulate,

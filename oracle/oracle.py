@@ -81,6 +81,7 @@ def _declare(l):
         "or_action_loops": ([_P, _P, _D, _D], _D),
         "or_force_loops": ([_P, _P, _D, _D, _P], None),
         "or_polyakov_loop": ([_P, _P, _P], None),
+        "or_dsdu_loops": ([_P, _P, _D, _D, _P], None),
         "or_stout_force_loops": ([_P, _P, _I, _P, _D, _D, _P], None),
         "or_stout_action_loops": ([_P, _P, _I, _P, _D, _D], _D),
         "or_loop_staple_count": ([_I, _I], _I),
@@ -295,6 +296,15 @@ def force_loops(L, U, c_plaq, c_rect):
     F = new_mom(L)
     lib().or_force_loops(_ptr(_L(L)), _ptr(U), float(c_plaq), float(c_rect), _ptr(F))
     return F
+
+
+def dsdu_loops(L, U, c_plaq, c_rect):
+    """dS/dU_mu(x) = c_plaq (plaquette staples) + c_rect (rectangle staples)
+    of every link, links layout."""
+    _chk(U, np.complex128)
+    D = new_links(L)
+    lib().or_dsdu_loops(_ptr(_L(L)), _ptr(U), float(c_plaq), float(c_rect), _ptr(D))
+    return D
 
 
 def stout_force_loops(L, U, rho, c_plaq, c_rect):

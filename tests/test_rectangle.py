@@ -87,6 +87,62 @@ def test_smeared_iwasaki_md_is_reversible(oracle):
                                  + oracle.kinetic(list(L4), P0) / 2, rel=1e-14)
 
 
+def _rect_table():
+    """The double-float rectangle kernel's product table (c_rect_ops of
+    gf_rect.cu), parsed from the source."""
+    import os
+    import re
+    src = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "gaugefields.jl_gb300",
+                            "csrc", "gf_rect.cu")).read()
+    block = src[src.index("__constant__ DfOpR c_rect_ops[28]"):]
+    block = block[:block.index("};")]
+    ops = [tuple(int(v) for v in m.group(1).split(","))
+           for m in re.finditer(r"\{(-?\d+(?:,\s*-?\d+){11})\}", block)]
+    assert len(ops) == 28
+    return ops
+
+
+def test_double_float_rectangle_table_builds_the_loop_staples(oracle):
+    """The table of k_force_rect_df (28 products per plane: the two
+    plaquette staples into S, the six rectangle staples into R), run on the
+    host in complex128 with its own operand rules (link of direction mu or nu
+    at x + mo mu + no nu, optionally daggered, or the running product t),
+    gives cp S + cr R equal to the oracle's loop-set dS/dU to 1e-13: the
+    table holds exactly the rectangles of make_rect and the plaquette staples."""
+    L = list(L4)
+    U = oracle.hot_start(L, 9)
+    M = oracle.mats(U)
+    ref = oracle.mats(oracle.dsdu_loops(L, U, CP, CR))
+    ops = _rect_table()
+    V = int(np.prod(L))
+
+    def site(x, mu, a, nu, b):
+        c = [x % L[0], (x // L[0]) % L[1], (x // (L[0] * L[1])) % L[2], x // (L[0] * L[1] * L[2])]
+        c[mu] = (c[mu] + a) % L[mu]
+        c[nu] = (c[nu] + b) % L[nu]
+        return c[0] + L[0] * (c[1] + L[1] * (c[2] + L[2] * c[3]))
+
+    worst = 0.0
+    for mu in range(4):
+        for x in range(0, V, 7):
+            slots = [np.zeros((3, 3), complex) for _ in range(3)]
+            for k in range(1, 4):
+                nu = (mu + k) % 4
+
+                def operand(src, d, mo, no, dag):
+                    m = slots[0] if src == 1 else M[nu if d else mu, site(x, mu, mo, nu, no)]
+                    return m.conj().T if dag else m
+
+                for op in ops:
+                    a = operand(*op[0:5])
+                    b = operand(*op[5:10])
+                    r = a @ b
+                    slots[op[10]] = (slots[op[10]] + r) if op[11] else r
+            T = CP * slots[1] + CR * slots[2]
+            worst = max(worst, np.abs(T - ref[mu, x]).max())
+    assert worst < 1e-13
+
+
 def test_rectangle_sum_is_gauge_invariant(oracle):
     from test_oracle import oracle_shift
     U = oracle.hot_start(list(L4), 21)
